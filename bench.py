@@ -1,0 +1,305 @@
+#!/usr/bin/env python3
+"""Throughput of the atmosphere step: cell-steps/s on the precision-form workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload precision-512x512x256] [--mode plain|mixed|both]
+
+One step = one environmentGPU::updateGPU of the whole grid (ground, diffusion, PPM advection,
+buoyancy, projection, sedimentation, microphysics). Synthetic seeded soundings stand in for the
+reference's radiosonde input. Every field is larger than L2 (268 MB per field at 512x256x512),
+so timed steps do not reuse L2 contents between steps.
+
+Printed JSON line (rank 0): value = whole-job cell-steps/s with the state resident in HBM
+(CUDA events on the library stream); e2e = the same metric through the C ABI from host
+buffers (init H2D + per-step readback of every prognostic field, as the reference's per-step
+GPUSetEnv does); roofline = the dominant kernel's algorithmic bytes / its event-timed launch
+duration against the measured HBM copy bandwidth; cpu_baseline = the oracle (CPU restatement)
+on the host cores on a bounded sub-box sample.
+
+Multi-GPU: the path does not shard (one domain per GPU); N>1 runs N independent replicas, one
+per rank, with no collective on the data path ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "cell-steps/s at 512x512x256, mixed vs plain PCG at 1e-5 rel err; % HBM roofline"
+
+# Algorithmic bytes per cell per launch of each profiled stage (FP32 fields; each array counted
+# once per launch; neighbour re-reads excluded).
+STAGE_BYTES = {
+    "pcg_matvec": 24.0,   # s, ax, ay, az, aw read; As write
+    "pcg_update": 28.0,   # p, r read+write; s, As, aw read
+    "pcg_search": 16.0,   # r, aw read; s read+write
+    "diffuse": 8.0,       # per sweep: in read, out write
+    "advect": 12.0,       # per pass: q, vel read; out write
+    "micro": 64.0,        # 6 Q + th read/write, rho, p read (fused addHeat)
+    "buoyancy": 36.0,
+    "eos": 16.0,
+    "proj_setup": 48.0,
+    "proj_apply": 44.0,
+}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def pinned_like(a):
+    """A pinned host copy of a numpy array when torch is present (host->device from pinned)."""
+    try:
+        import torch
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t.numpy(), t
+    except Exception:
+        return np.ascontiguousarray(a), None
+
+
+def cpu_baseline(workload: str, sample_shape, steps: int = 1):
+    """The oracle (CPU restatement of the reference, OpenMP on all host cores) on a sub-box."""
+    import oracle
+    from skewtcloudsim_gb300 import sounding
+    init, dt, speed = sounding.workload(workload, scale=sample_shape)
+    st = oracle.OracleState(init, np.float32)
+    cfg = oracle.Config()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st.step(cfg, dt, speed)
+    el = time.perf_counter() - t0
+    cells = init.nx * init.ny * init.nz
+    return {"value": cells * steps / el, "unit": "cell-steps/s", "cores": oracle.lib().oc_num_threads(),
+            "kind": "port",
+            "sample": f"{steps} step(s) of the same workload on a {sample_shape[0]}x{sample_shape[1]}x{sample_shape[2]} "
+                      f"(x,y,z; z vertical) sub-box, reference semantics, FP32, {el:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sample = (128, 128, 64)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, sample, 1)
+    t_all = []
+    for _ in range(args.steps):
+        r = cpu_baseline(args.workload, sample, 1)
+        vals.append(r["value"])
+        t_all.append(1.0 / r["value"])
+    v = float(np.median(vals))
+    out = {"metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+           "config": {"workload": args.workload, "sample": "128x128x64 sub-box per step", "parallelism": "replicas"},
+           "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": r["cores"], "kind": "port",
+                            "sample": r["sample"]},
+           "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="precision-512x512x256")
+    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--semantics", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    from skewtcloudsim_gb300 import Environment, SolverConfig, sounding, build
+    build.build()
+
+    init, dt, speed = sounding.workload(args.workload)
+    cfg = SolverConfig(semantics=args.semantics, precision=1 if args.mode == "mixed" else 0)
+    env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
+    env.init_from(init)
+    cells = init.nx * init.ny * init.nz
+
+    for _ in range(args.warmup):
+        env.update_gpu(dt, speed)
+    env.sync()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----------------------------------------------------
+    barrier()
+    l0 = env.stats()["kernel_launches"]
+    iters = []
+    with ClockSampler(local) as clk:
+        env.update_gpu(dt, speed, nsteps=args.steps)
+        barrier()
+    st = env.stats()
+    ms_total = st["gpu_ms"]
+    launches = st["kernel_launches"] - l0
+    if pg:
+        t = torch.tensor([ms_total], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_per_step = ms_total / args.steps
+    value = cells * args.steps * world / (ms_total / 1e3)
+
+    # ---- per-stage profile of one more step (not timed) ----------------------------------
+    env.profile(True)
+    env.update_gpu(dt, speed)
+    prof = env.profile_read()
+    env.profile(False)
+    pcg_iters = env.stats()["pcg_iters"]
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    dname, d = dom
+    per_launch_ms = d["ms"] / max(d["kernels"], 1)
+    peak, peak_kind = measured_peak()
+    bpc = STAGE_BYTES.get(dname)
+    roofline = None
+    if bpc:
+        achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
+        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "traffic": None, "kernel": dname,
+                    "bytes_per_cell": bpc, "peak_source": peak_kind}
+    step_ms_prof = sum(v["ms"] for v in prof.values())
+
+    # ---- end to end through the C ABI from host buffers ----------------------------------
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        names = ("th", "qv", "qw", "qc", "qr", "qs", "qi", "u", "v", "w", "p")
+        host_in = {k: pinned_like(getattr(init, k)) for k in ("theta", "vel", "qv", "ground_T", "ground_p", "p3d",
+                                                               "p_column")}
+        outs = {k: pinned_like(np.empty(cells, np.float32)) for k in names}
+        env2 = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
+        K = args.steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        env2.init(host_in["theta"][0], host_in["vel"][0], host_in["qv"][0], host_in["ground_T"][0],
+                  host_in["ground_p"][0], host_in["p3d"][0], host_in["p_column"][0], init.ground_height)
+        for _ in range(K):
+            env2.update_gpu(dt, speed)
+            for k in names:
+                a = outs[k][0]
+                prm, dr = __import__("skewtcloudsim_gb300").FIELDS[k]
+                env2._check(env2._L.skt_read_field(env2._h, int(prm), int(dr),
+                                                   a.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_float)),
+                                                   a.size))
+        el = time.perf_counter() - t0
+        h2d = sum(a[0].nbytes for a in host_in.values()) + init.ground_height.nbytes
+        d2h = len(names) * cells * 4
+        e2e = {"value": cells * K / el, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d / K),
+               "d2h_bytes_per_step": int(d2h), "steps": K,
+               "note": "init from pinned host arrays once, then each step followed by the readback of the 11 "
+                       "prognostic fields (the reference's per-step GPUSetEnv); host wall clock"}
+        env2.close()
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline(args.workload, (128, 128, 64), 1)
+
+    out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": args.workload, "grid_xyz": [init.nx, init.nz, init.ny], "cells": cells,
+                      "dt": dt, "pcg": args.mode, "semantics": "reference" if args.semantics == 0 else "textbook",
+                      "pcg_iters_per_step": pcg_iters, "l2": "inputs larger than L2 (268 MB per field)",
+                      "parallelism": "replicas" if world > 1 else "single"},
+           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+           "clocks": clk.summary(), "profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+           "profile_step_ms": round(step_ms_prof, 3)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    env.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,171 @@
+/*
+ * skewt.h — C ABI of libskewt_gb300, a GB300 (sm_103a) implementation of skewTCloudSim's
+ * per-timestep 3D atmosphere solver: colour-split diffusion, PPM advection, sedimentation,
+ * buoyancy, a PCG pressure projection, bulk six-species microphysics and the ground/surface
+ * kernels.
+ *
+ * It replaces the reference's `environmentGPU` class (Game/environment.cuh:9-183,
+ * Game/environment.cu:71-1300). Plain pointers and sizes only. The library owns every device
+ * buffer; host arrays passed in are copied.
+ *
+ * Layout: fields are float32 arrays of nx*ny*nz cells, idx = x + y*nx + z*nx*ny with y
+ * VERTICAL (the reference's layout, Game/utils.cuh:8-11). Ground arrays hold nx*nz values,
+ * idxG = x + z*nx. Cell (x,y,z) is ground when y <= ground_height[idxG].
+ *
+ * Threading: calls on one skt_env are not thread-safe; different environments are
+ * independent. Work is queued on the environment's own CUDA stream. Nothing aborts the process:
+ * every call returns an skt_status, and skt_last_error() describes the last failure.
+ */
+#ifndef SKEWT_GB300_H
+#define SKEWT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct skt_env skt_env;
+
+typedef enum {
+    SKT_OK = 0,
+    SKT_INVALID_ARG = 1,
+    SKT_CUDA_ERROR = 2,
+    SKT_NOT_CONVERGED = 3, /* the PCG hit its iteration cap; the step still completed */
+    SKT_NAN_DETECTED = 4,
+    SKT_TIMEOUT = 5,
+    SKT_OUT_OF_MEMORY = 6,
+    SKT_NOT_INITIALIZED = 7,
+    SKT_COURANT_LIMIT = 8  /* more Courant substeps were needed than the captured step holds */
+} skt_status;
+
+/* Field selector, the reference's `parameter` enum (Game/config.h:62-65) plus DENSITY. */
+typedef enum {
+    SKT_POTTEMP = 0, SKT_QV = 1, SKT_QW = 2, SKT_QC = 3, SKT_QR = 4, SKT_QS = 5, SKT_QI = 6,
+    SKT_WIND = 7, SKT_PGROUND = 8, SKT_PRESSURE = 9, SKT_DEBUG1 = 10, SKT_DEBUG2 = 11, SKT_DEBUG3 = 12,
+    SKT_DENSITY = 100
+} skt_param;
+
+/* Wind component selector, the reference's `direction` enum (Game/config.h:36-39):
+ * LEFT/RIGHT = u (x), UP/DOWN = v (vertical), FORWARD/BACKWARD = w (z). */
+typedef enum { SKT_LEFT = 0, SKT_RIGHT = 1, SKT_UP = 2, SKT_DOWN = 3, SKT_FORWARD = 4, SKT_BACKWARD = 5 } skt_direction;
+
+/* Ground (nx*nz) arrays, gridDataGroundGPU (Game/environment.cuh:28-37) plus cloud cover. */
+typedef enum {
+    SKT_G_QRS = 0, SKT_G_QGR = 1, SKT_G_QGS = 2, SKT_G_QGI = 3, SKT_G_P = 4, SKT_G_TIME_WET = 5, SKT_G_T = 6,
+    SKT_G_CLOUD_COVER = 7
+} skt_ground_field;
+
+/* Per-level default columns (ny values) taken at init. */
+typedef enum { SKT_C_ISEN_T = 0, SKT_C_ISEN_QV = 1, SKT_C_DEF_U = 2, SKT_C_DEF_W = 3 } skt_column;
+
+typedef struct {
+    int nx, ny, nz; /* ny is vertical */
+    float voxel;    /* cell size in metres (the reference's VOXELSIZE, Game/config.h:9) */
+} skt_grid_desc;
+
+typedef enum { SKT_SEM_REFERENCE = 0, SKT_SEM_TEXTBOOK = 1 } skt_semantics;
+typedef enum { SKT_PCG_PLAIN = 0, SKT_PCG_MIXED = 1 } skt_precision;
+
+typedef struct {
+    int semantics;      /* skt_semantics: REFERENCE reproduces the reference's PCG quirks */
+    int diffuse_sweeps; /* Jacobi sweeps per field (20, Game/environment.cu:649) */
+    float pcg_tol;      /* stop when the max residual <= tol (1e-5, Game/environment.cu:906) */
+    int pcg_max_iter;   /* 200 (Game/environment.cu:907) */
+    int max_substeps;   /* Courant substep cap (100, Game/environment.cu:727) */
+    int precision;      /* skt_precision */
+    float refine_tol;   /* MIXED: relative residual target of the FP64 refinement (1e-8) */
+    int inner_max_iter; /* MIXED: FP32 iterations per refinement step */
+    float inner_rtol;   /* MIXED: relative tolerance of each FP32 inner solve */
+    int use_graph;      /* capture the step in a CUDA graph (substep slots = max_substeps) */
+} skt_solver_cfg;
+
+typedef struct {
+    int pcg_iters;        /* iterations of the last step's projection (total inner for MIXED) */
+    float pcg_residual;   /* final max residual */
+    int pcg_converged;    /* 1 when the tolerance was met */
+    int nsub[10];         /* Courant substeps per advected field (theta,u,v,w,qv,qw,qc,qr,qs,qi) */
+    int outer_iters;      /* MIXED: refinement steps */
+    double sim_time;      /* environmentGPU::m_time */
+    long long kernel_launches; /* kernels this environment has launched since skt_create */
+    float gpu_ms;         /* device time of the last skt_step call (CUDA events on its stream) */
+} skt_step_stats;
+
+/* Fills cfg with the reference's settings (reference semantics, plain PCG, no graph). */
+void skt_default_config(skt_solver_cfg* cfg);
+
+/* Replaces environmentGPU::environmentGPU() (Game/environment.cu:71-185): allocates all device
+ * state for one grid on the current CUDA device and sets the ground stores as the reference
+ * constructor does (Qrs = 0.001, P = 1000 hPa, T = 315.15 K, others 0). */
+skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_env** out);
+
+/* Replaces environmentGPU::~environmentGPU() (Game/environment.cu:187-247). NULL is accepted. */
+void skt_destroy(skt_env* env);
+
+#define SKT_INIT_NOISE 1u /* add the reference's init noise (Game/environment.cu:308-313) */
+
+/* Replaces environmentGPU::init (Game/environment.cu:249-389, declared
+ * Game/environment.cuh:42). vel_aos3 holds (u, v, w) per cell on MAC faces like the reference's
+ * glm::vec3 array; ground_height replaces the Perlin heightfield (which rounds to a flat ground
+ * layer in the reference); noise_seed is the first of the five randomArray seeds (100). */
+skt_status skt_init(skt_env* env, const float* theta, const float* vel_aos3, const float* qv, const float* ground_T,
+                    const float* ground_p, const float* p3d, const float* p_column, const int32_t* ground_height,
+                    uint32_t flags, uint32_t noise_seed);
+
+/* Replaces environmentGPU::updateGPU(dt, speed) (Game/environment.cu:391-555), nsteps times.
+ * Returns SKT_NOT_CONVERGED when a projection hit its iteration cap (the step is still done, as
+ * in the reference). Does not read fields back (the reference's per-step GPUSetEnv copy,
+ * Game/environment.cu:553, is explicit here: skt_read_field). */
+skt_status skt_step(skt_env* env, float dt, float speed, int nsteps);
+
+/* Waits for the environment's stream. */
+skt_status skt_sync(skt_env* env);
+
+/* Field readback: the per-field copies of editor::GPUSetEnv (Game/editor.cpp:226-260).
+ * dir selects the wind component for SKT_WIND. n must equal nx*ny*nz. Synchronous. */
+skt_status skt_read_field(skt_env* env, int param, int dir, float* host_dst, size_t n);
+
+/* Field upload (state injection); same selectors. Synchronous. */
+skt_status skt_write_field(skt_env* env, int param, int dir, const float* host_src, size_t n);
+
+/* Replaces environmentGPU::getParamArray (Game/environment.cu:1076-1125): the device pointer of
+ * a field, valid until skt_destroy. */
+skt_status skt_field_device_ptr(skt_env* env, int param, int dir, float** out);
+
+/* Ground arrays (nx*nz) and default columns (ny). Synchronous. */
+skt_status skt_read_ground(skt_env* env, int which, float* host_dst, size_t n);
+skt_status skt_write_ground(skt_env* env, int which, const float* host_src, size_t n);
+skt_status skt_read_column(skt_env* env, int which, float* host_dst, size_t n);
+skt_status skt_write_column(skt_env* env, int which, const float* host_src, size_t n);
+
+/* Diurnal clock of environmentGPU (m_time, m_day, m_longitude, m_sunStrength, m_pauseDiurnal). */
+skt_status skt_set_clock(skt_env* env, double sim_time, int day, float longitude, float sun, int pause);
+
+/* Diagnostics of the last step (PCG iterations/residual, substeps). */
+skt_status skt_stats(skt_env* env, skt_step_stats* out);
+
+/* Runs one stage of the step alone, for per-stage parity tests:
+ * 0 diffuse (arg = type 0..5 on theta,qv,u,v,w,qw), 1 advect (arg 0..5 on theta,u,v,w,qv,qw),
+ * 2 buoyancy, 3 density + projection, 4 microphysics, 5 sedimentation (arg 0..2 on qr,qs,qi),
+ * 6 ground stage, 8 density, 9 pressure from density. dt is dt*speed except for 4 and 6. */
+skt_status skt_run_stage(skt_env* env, int stage, int arg, float dt, float speed, skt_step_stats* out);
+
+/* Per-stage CUDA-event timing of the kernels queued while enabled (no reference
+ * counterpart; the reference's own timing code is commented out, Game/environment.cu:697-702).
+ * skt_profile_read synchronises, then writes a JSON object {stage: [ms, kernels, scopes]} into
+ * buf and clears the records. */
+skt_status skt_profile_enable(skt_env* env, int on);
+skt_status skt_profile_read(skt_env* env, char* buf, size_t n);
+
+/* Text of the last error on env (or of the last skt_create failure when env is NULL). */
+const char* skt_last_error(const skt_env* env);
+
+/* Library version string. */
+const char* skt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKEWT_GB300_H */

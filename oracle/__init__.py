@@ -1,0 +1,166 @@
+"""ORACLE — test infrastructure only.
+
+CPU restatement of skewTCloudSim's atmosphere step (skt_oracle.cpp), loaded through ctypes.
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use this module; the
+product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libskt_oracle.so")
+
+SKY_FIELDS = ("th", "qv", "qw", "qc", "qr", "qs", "qi", "u", "v", "w", "p", "rho")
+GROUND_FIELDS = ("Qrs", "Qgr", "Qgs", "Qgi", "Pg", "tg", "Tg")
+COLUMN_FIELDS = ("isenT", "isenQv", "defU", "defW")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (-ffp-contract=off so x86 and Arm give the same bits)."""
+    src = os.path.join(HERE, "skt_oracle.cpp")
+    hdr = os.path.join(HERE, "skt_oracle_physics.hpp")
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-fno-fast-math", src, "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class OcConfig(ctypes.Structure):
+    _fields_ = [("semantics", ctypes.c_int), ("diffuse_sweeps", ctypes.c_int), ("pcg_tol", ctypes.c_float),
+                ("pcg_max_iter", ctypes.c_int), ("max_substeps", ctypes.c_int), ("voxel", ctypes.c_float)]
+
+
+class OcState(ctypes.Structure):
+    _fields_ = ([(n, ctypes.c_void_p) for n in SKY_FIELDS + GROUND_FIELDS + COLUMN_FIELDS] +
+                [("gh", ctypes.c_void_p), ("sim_time", ctypes.c_double), ("day", ctypes.c_int),
+                 ("longitude", ctypes.c_float), ("sun", ctypes.c_float), ("pause", ctypes.c_int)])
+
+
+class OcDiag(ctypes.Structure):
+    _fields_ = [("pcg_iters", ctypes.c_int), ("pcg_residual", ctypes.c_double),
+                ("nsub", ctypes.c_int * 10), ("converged", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        for suf in ("f32", "f64"):
+            f = getattr(L, f"oc_step_{suf}")
+            f.argtypes = [ctypes.POINTER(OcConfig), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                          ctypes.POINTER(OcState), ctypes.c_float, ctypes.c_float, ctypes.POINTER(OcDiag)]
+            f.restype = ctypes.c_int
+            g = getattr(L, f"oc_init_{suf}")
+            g.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_int]
+            g.restype = ctypes.c_int
+        L.oc_stage_f32.argtypes = [ctypes.POINTER(OcConfig), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(OcState), ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                   ctypes.c_float, ctypes.POINTER(OcDiag)]
+        L.oc_stage_f32.restype = ctypes.c_int
+        L.oc_irradiance.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
+        L.oc_irradiance.restype = ctypes.c_float
+        L.oc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+@dataclass
+class Config:
+    semantics: int = 0          # 0 reference, 1 textbook
+    diffuse_sweeps: int = 20
+    pcg_tol: float = 1e-5
+    pcg_max_iter: int = 200
+    max_substeps: int = 100
+
+    def c(self, voxel):
+        return OcConfig(self.semantics, self.diffuse_sweeps, self.pcg_tol, self.pcg_max_iter,
+                        self.max_substeps, voxel)
+
+
+class OracleState:
+    """All prognostic arrays of one environment, in float32 or float64."""
+
+    def __init__(self, init, dtype=np.float32, noise: bool = True):
+        self.dtype = np.dtype(dtype)
+        self.X, self.Y, self.Z = init.nx, init.ny, init.nz
+        self.voxel = init.voxel
+        n, ng = self.X * self.Y * self.Z, self.X * self.Z
+        vel = init.vel.reshape(n, 3)
+        a = {}
+        a["th"] = init.theta.astype(dtype).copy()
+        a["qv"] = init.qv.astype(dtype).copy()
+        for k in ("qw", "qc", "qr", "qs", "qi", "rho"):
+            a[k] = np.zeros(n, dtype)
+        a["u"] = vel[:, 0].astype(dtype).copy()
+        a["v"] = vel[:, 1].astype(dtype).copy()
+        a["w"] = vel[:, 2].astype(dtype).copy()
+        a["p"] = init.p3d.astype(dtype).copy()
+        a["Qrs"] = np.full(ng, 0.001, dtype)
+        for k in ("Qgr", "Qgs", "Qgi", "tg"):
+            a[k] = np.zeros(ng, dtype)
+        a["Pg"] = init.ground_p.astype(dtype).copy()
+        a["Tg"] = init.ground_T.astype(dtype).copy()
+        for k in COLUMN_FIELDS:
+            a[k] = np.zeros(self.Y, dtype)
+        self.a = a
+        self.gh = np.ascontiguousarray(init.ground_height, np.int32).copy()
+        self.sim_time = 43200.0
+        self.day, self.longitude, self.sun, self.pause = 130, 52.37, 1.0, 0
+        st = self._cstate()
+        fn = lib().oc_init_f32 if self.dtype == np.float32 else lib().oc_init_f64
+        fn(self.X, self.Y, self.Z, ctypes.byref(st), int(noise))
+
+    def _cstate(self):
+        st = OcState()
+        for k, v in self.a.items():
+            setattr(st, k, v.ctypes.data)
+        st.gh = self.gh.ctypes.data
+        st.sim_time, st.day, st.longitude, st.sun, st.pause = self.sim_time, self.day, self.longitude, self.sun, self.pause
+        return st
+
+    def step(self, cfg: Config, dt: float, speed: float = 1.0):
+        st = self._cstate()
+        d = OcDiag()
+        fn = lib().oc_step_f32 if self.dtype == np.float32 else lib().oc_step_f64
+        c = cfg.c(self.voxel)
+        rc = fn(ctypes.byref(c), self.X, self.Y, self.Z, ctypes.byref(st), dt, speed, ctypes.byref(d))
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed: {rc}")
+        self.sim_time = st.sim_time
+        return {"pcg_iters": d.pcg_iters, "pcg_residual": d.pcg_residual, "nsub": list(d.nsub),
+                "converged": bool(d.converged)}
+
+    def stage(self, cfg: Config, stage: int, arg: int = 0, dt: float = 0.5, speed: float = 1.0):
+        assert self.dtype == np.float32
+        st = self._cstate()
+        d = OcDiag()
+        c = cfg.c(self.voxel)
+        rc = lib().oc_stage_f32(ctypes.byref(c), self.X, self.Y, self.Z, ctypes.byref(st), stage, arg, dt, speed,
+                                ctypes.byref(d))
+        if rc != 0:
+            raise RuntimeError(f"oracle stage failed: {rc}")
+        return {"pcg_iters": d.pcg_iters, "pcg_residual": d.pcg_residual, "nsub": d.nsub[0]}
+
+    def sky_mask(self):
+        y = np.arange(self.Y)[None, :, None]
+        gh = self.gh.reshape(self.Z, self.X)[:, None, :]
+        return (y > gh).reshape(-1)
+
+    def field(self, name):
+        return self.a[name]

@@ -1,0 +1,12 @@
+"""skewtcloudsim_gb300: GB300-native per-timestep 3D atmosphere solver of skewTCloudSim.
+
+The compute path is libskewt_gb300.so (hand-written CUDA for sm_103a behind the C ABI in
+include/skewt.h). This package holds the host-side mirror of the reference's environmentGPU
+(``Environment``), the synthetic sounding generator and the build recipe.
+"""
+from .environment import (Environment, SolverConfig, Parameter, Direction, Ground, Column, Status,
+                          SktError, FIELDS, GROUND_FIELDS, COLUMNS)
+from . import sounding
+
+__all__ = ["Environment", "SolverConfig", "Parameter", "Direction", "Ground", "Column", "Status", "SktError",
+           "FIELDS", "GROUND_FIELDS", "COLUMNS", "sounding"]

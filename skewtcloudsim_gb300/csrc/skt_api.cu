@@ -1,0 +1,505 @@
+// C ABI of libskewt_gb300 and the host orchestration of one step
+// (environmentGPU, Game/environment.cu:71-1300).
+#include "skt_internal.cuh"
+#include "../../include/skewt.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace skt;
+
+struct skt_env {
+    Env e;
+};
+
+namespace {
+
+thread_local std::string g_create_err;
+
+skt_status fail(Env* e, skt_status st, const std::string& msg) {
+    if (e) e->err = msg;
+    else g_create_err = msg;
+    return st;
+}
+
+skt_status cuda_check(Env& e, const char* where) {
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        e.err = std::string(where) + ": " + cudaGetErrorString(err);
+        return err == cudaErrorMemoryAllocation ? SKT_OUT_OF_MEMORY : SKT_CUDA_ERROR;
+    }
+    return SKT_OK;
+}
+
+// irridianceGPU Game/environment.cu:1021-1034 (host, float)
+float irradiance(float time, int day, float longitude, float sun) {
+    const float Gs = 1361.0f * sun;
+    const float rd = 1 + 0.034f * cosf(2 * 3.14159265359f * day / 365);
+    const float sd = 0.409f * sinf(2 * 3.14159265359f / 365 * (day - 81));
+    const float th = time / 3600;
+    const float lr = longitude * 0.01745329251994329576923690768489f;  // glm::radians
+    const float sr = (th - (6.0f + 14.0f / 2.0f)) * (3.14159265359f / 12.0f);
+    const float v = Gs * rd * (sinf(lr) * sinf(sd) + cosf(lr) * cosf(sd) * cosf(sr));
+    return v > 0.0f ? v : 0.0f;
+}
+
+__global__ void k_fill(float* a, float v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+float* sky_ptr(Env& e, int param, int dir) {
+    switch (param) {
+        case SKT_POTTEMP: return e.th;
+        case SKT_QV: return e.qv;
+        case SKT_QW: return e.qw;
+        case SKT_QC: return e.qc;
+        case SKT_QR: return e.qr;
+        case SKT_QS: return e.qs;
+        case SKT_QI: return e.qi;
+        case SKT_WIND:
+            if (dir == SKT_LEFT || dir == SKT_RIGHT) return e.u;
+            if (dir == SKT_UP || dir == SKT_DOWN) return e.v;
+            if (dir == SKT_FORWARD || dir == SKT_BACKWARD) return e.w;
+            return nullptr;
+        case SKT_PRESSURE: return e.p;
+        case SKT_DENSITY: return e.rho;
+        default: return nullptr;
+    }
+}
+float* ground_ptr(Env& e, int which) {
+    switch (which) {
+        case SKT_G_QRS: return e.Qrs;
+        case SKT_G_QGR: return e.Qgr;
+        case SKT_G_QGS: return e.Qgs;
+        case SKT_G_QGI: return e.Qgi;
+        case SKT_G_P: return e.Pg;
+        case SKT_G_TIME_WET: return e.tg;
+        case SKT_G_T: return e.Tg;
+        case SKT_G_CLOUD_COVER: return e.cover;
+        default: return nullptr;
+    }
+}
+float* column_ptr(Env& e, int which) {
+    switch (which) {
+        case SKT_C_ISEN_T: return e.isenT;
+        case SKT_C_ISEN_QV: return e.isenQv;
+        case SKT_C_DEF_U: return e.defU;
+        case SKT_C_DEF_W: return e.defW;
+        default: return nullptr;
+    }
+}
+
+// One step in the reference's stage order (Game/environment.cu:391-555).
+skt_status run_step(Env& e, float dt, float speed) {
+    const float dtS = dt * speed;
+    const bool hs = true;
+    const float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
+    // ground, then setTempsAtGround (fused into the ground column kernel)
+    launch_ground(e, dt, speed, irr);
+    // theta
+    launch_diffuse(e, e.th, 0, dtS);
+    e.last_nsub[0] = launch_advect(e, e.th, e.isenT, CUSTOM, CUSTOM, dtS, 0, hs);
+    // momentum
+    launch_buoyancy(e, dtS);
+    launch_diffuse(e, e.u, 2, dtS);
+    launch_diffuse(e, e.v, 3, dtS);
+    launch_diffuse(e, e.w, 4, dtS);
+    e.last_nsub[1] = launch_advect(e, e.u, e.defU, CUSTOM, DIRICHLET, dtS, 1, hs);
+    e.last_nsub[2] = launch_advect(e, e.v, e.zeroY, DIRICHLET, DIRICHLET, dtS, 2, hs);
+    e.last_nsub[3] = launch_advect(e, e.w, e.defW, CUSTOM, DIRICHLET, dtS, 3, hs);
+    launch_init_density(e);
+    launch_project(e, dtS);
+    launch_new_pressure(e);
+    // moisture
+    launch_diffuse(e, e.qv, 1, dtS);
+    e.last_nsub[4] = launch_advect(e, e.qv, e.isenQv, CUSTOM, CUSTOM, dtS, 4, hs);
+    launch_diffuse(e, e.qw, 5, dtS);
+    e.last_nsub[5] = launch_advect(e, e.qw, e.zeroY, DIRICHLET, DIRICHLET, dtS, 5, hs);
+    launch_diffuse(e, e.qc, 5, dtS);
+    e.last_nsub[6] = launch_advect(e, e.qc, e.zeroY, DIRICHLET, DIRICHLET, dtS, 6, hs);
+    launch_diffuse(e, e.qr, 5, dtS);
+    launch_precip(e, e.qr, 0, dtS);
+    e.last_nsub[7] = launch_advect(e, e.qr, e.zeroY, DIRICHLET, DIRICHLET, dtS, 7, hs);
+    launch_diffuse(e, e.qs, 5, dtS);
+    launch_precip(e, e.qs, 1, dtS);
+    e.last_nsub[8] = launch_advect(e, e.qs, e.zeroY, DIRICHLET, DIRICHLET, dtS, 8, hs);
+    launch_diffuse(e, e.qi, 5, dtS);
+    launch_precip(e, e.qi, 2, dtS);
+    e.last_nsub[9] = launch_advect(e, e.qi, e.zeroY, DIRICHLET, DIRICHLET, dtS, 9, hs);
+    // microphysics + latent heat
+    launch_micro(e, dt, speed);
+    // clock (m_time, Game/environment.cu:550-551)
+    e.sim_time += speed * dt * float(!e.pause);
+    if (e.sim_time > 86400.0f) e.sim_time = 0.0f;
+    return cuda_check(e, "step");
+}
+
+}  // namespace
+
+extern "C" {
+
+void skt_default_config(skt_solver_cfg* c) {
+    if (!c) return;
+    c->semantics = SKT_SEM_REFERENCE;
+    c->diffuse_sweeps = 20;
+    c->pcg_tol = 1e-5f;
+    c->pcg_max_iter = 200;
+    c->max_substeps = 100;
+    c->precision = SKT_PCG_PLAIN;
+    c->refine_tol = 1e-8f;
+    c->inner_max_iter = 60;
+    c->inner_rtol = 1e-3f;
+    c->use_graph = 0;
+}
+
+const char* skt_version(void) { return "skewt-gb300 0.1 (sm_103a)"; }
+
+const char* skt_last_error(const skt_env* env) { return env ? env->e.err.c_str() : g_create_err.c_str(); }
+
+skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_env** out) {
+    if (!grid || !out) return fail(nullptr, SKT_INVALID_ARG, "null argument");
+    *out = nullptr;
+    const long long n = (long long)grid->nx * grid->ny * grid->nz;
+    if (grid->nx < 1 || grid->ny < 2 || grid->nz < 1 || n >= (1ll << 31) || !(grid->voxel > 0.0f))
+        return fail(nullptr, SKT_INVALID_ARG, "invalid grid (need nx,nz >= 1, ny >= 2, nx*ny*nz < 2^31, voxel > 0)");
+    skt_solver_cfg c;
+    skt_default_config(&c);
+    if (cfg) c = *cfg;
+    if (c.diffuse_sweeps < 0 || c.pcg_max_iter < 0 || c.max_substeps < 1 || (c.semantics != 0 && c.semantics != 1) ||
+        (c.precision != 0 && c.precision != 1))
+        return fail(nullptr, SKT_INVALID_ARG, "invalid solver configuration");
+    skt_env* h = new (std::nothrow) skt_env();
+    if (!h) return fail(nullptr, SKT_OUT_OF_MEMORY, "host allocation failed");
+    Env& e = h->e;
+    cudaGetDevice(&e.device);
+    cudaDeviceGetAttribute(&e.num_sms, cudaDevAttrMultiProcessorCount, e.device);
+    e.g.X = grid->nx;
+    e.g.Y = grid->ny;
+    e.g.Z = grid->nz;
+    e.g.XY = grid->nx * grid->ny;
+    e.g.N = int(n);
+    e.g.vox = grid->voxel;
+    e.cfg = SolverCfg{c.semantics, c.diffuse_sweeps, c.pcg_tol, c.pcg_max_iter, c.max_substeps, c.precision, c.refine_tol, c.inner_max_iter,
+                      c.inner_rtol, c.use_graph};
+    const size_t N = size_t(n), NG = size_t(grid->nx) * grid->nz, NY = size_t(grid->ny);
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const int nsky = 12 + 2 + 4 + 4;
+    size_t bytes = al(N * 4) * nsky + al(N * 8) * 2 + al(NG * 4) * 10 + al(NG * 4) + al(NY * 4) * 5 + al(sizeof(Scalars)) +
+                   al(sizeof(double) * 2 * kMaxPartials);
+    if (cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        const std::string m = std::string("stream: ") + cudaGetErrorString(cudaGetLastError());
+        delete h;
+        return fail(nullptr, SKT_CUDA_ERROR, m);
+    }
+    if (cudaMalloc(&e.pool, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(e.stream);
+        delete h;
+        return fail(nullptr, SKT_OUT_OF_MEMORY, "device allocation of " + std::to_string(bytes) + " bytes failed");
+    }
+    e.pool_bytes = bytes;
+    char* p = (char*)e.pool;
+    auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
+    float** sky[nsky] = {&e.th, &e.qv, &e.qw, &e.qc, &e.qr, &e.qs, &e.qi, &e.u, &e.v, &e.w, &e.p, &e.rho,
+                         &e.tA, &e.tB, &e.r, &e.s, &e.As, &e.pp, &e.ax, &e.ay, &e.az, &e.aw};
+    for (int i = 0; i < nsky; ++i) *sky[i] = (float*)take(N * 4);
+    e.xd = (double*)take(N * 8);
+    e.rd = (double*)take(N * 8);
+    float** gr[10] = {&e.Qrs, &e.Qgr, &e.Qgs, &e.Qgi, &e.Pg, &e.tg, &e.Tg, &e.cover, &e.g2a, &e.g2b};
+    for (int i = 0; i < 10; ++i) *gr[i] = (float*)take(NG * 4);
+    e.gh = (int*)take(NG * 4);
+    float** co[5] = {&e.isenT, &e.isenQv, &e.defU, &e.defW, &e.zeroY};
+    for (int i = 0; i < 5; ++i) *co[i] = (float*)take(NY * 4);
+    e.sc = (Scalars*)take(sizeof(Scalars));
+    e.partials = (double*)take(sizeof(double) * 2 * kMaxPartials);
+    cudaMemsetAsync(e.pool, 0, bytes, e.stream);
+    e.g.gh = e.gh;
+    if (cudaMallocHost(&e.host_sc, sizeof(Scalars)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(e.pool);
+        cudaStreamDestroy(e.stream);
+        delete h;
+        return fail(nullptr, SKT_OUT_OF_MEMORY, "pinned allocation failed");
+    }
+    // the constructor's ground defaults (Game/environment.cu:162-168)
+    const int ng = int(NG);
+    k_fill<<<(ng + 255) / 256, 256, 0, e.stream>>>(e.Qrs, 0.001f, ng);
+    k_fill<<<(ng + 255) / 256, 256, 0, e.stream>>>(e.Pg, 1000.0f, ng);
+    k_fill<<<(ng + 255) / 256, 256, 0, e.stream>>>(e.Tg, 315.15f, ng);
+    // gammas (initGammasMicroPhysics Game/microPhysics.cu:31-61, initKernelSky Game/kernelSky.cu:30-37)
+    const float b = 0.8f, d = 0.25f;
+    e.gam.R = tgammaf(3 + b);
+    e.gam.ER = tgammaf((b + 5.0f) / 2.0f);
+    e.gam.S = tgammaf(3 + d);
+    e.gam.RC = tgammaf(6 + b);
+    e.gam.SS = tgammaf((d + 5.0f) / 2.0f);
+    e.gam.I = tgammaf(3.5f);
+    e.gam.RI = tgammaf(2.75f);
+    e.gam.Qr = tgammaf(4.0f + b);
+    e.gam.Qs = tgammaf(4.0f + d);
+    e.gam.Qi = e.gam.Qs;
+    const skt_status st = cuda_check(e, "create");
+    if (st != SKT_OK) {
+        g_create_err = e.err;
+        skt_destroy(h);
+        return st;
+    }
+    cudaStreamSynchronize(e.stream);
+    *out = h;
+    return SKT_OK;
+}
+
+void skt_destroy(skt_env* env) {
+    if (!env) return;
+    Env& e = env->e;
+    if (e.stream) cudaStreamSynchronize(e.stream);
+    if (e.graph_exec) cudaGraphExecDestroy(e.graph_exec);
+    if (e.ev0) cudaEventDestroy(e.ev0);
+    if (e.ev1) cudaEventDestroy(e.ev1);
+    if (e.pool) cudaFree(e.pool);
+    if (e.host_sc) cudaFreeHost(e.host_sc);
+    if (e.stream) cudaStreamDestroy(e.stream);
+    delete env;
+}
+
+skt_status skt_init(skt_env* env, const float* theta, const float* vel, const float* qv, const float* ground_T, const float* ground_p,
+                    const float* p3d, const float* p_column, const int32_t* gh, uint32_t flags, uint32_t noise_seed) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (!theta || !vel || !qv || !ground_T || !ground_p || !p3d || !gh) return fail(&e, SKT_INVALID_ARG, "null input array");
+    (void)p_column;  // the reference stores it for the editor only (m_defaultPressure)
+    const size_t N = size_t(e.g.N), NG = size_t(e.g.X) * e.g.Z;
+    for (size_t i = 0; i < NG; ++i)
+        if (gh[i] < 0 || gh[i] >= e.g.Y - 1)
+            return fail(&e, SKT_INVALID_ARG, "ground_height must lie in [0, ny-2] so every column has sky above the ground layer");
+    int flat = 1;
+    for (size_t i = 0; i < NG; ++i) flat &= gh[i] == 0;
+    e.flat = flat;
+    // AoS -> SoA (Game/environment.cu:263-281)
+    std::vector<float> u(N), v(N), w(N);
+    for (size_t i = 0; i < N; ++i) {
+        u[i] = vel[3 * i];
+        v[i] = vel[3 * i + 1];
+        w[i] = vel[3 * i + 2];
+    }
+    cudaMemcpyAsync(e.th, theta, N * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.u, u.data(), N * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.v, v.data(), N * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.w, w.data(), N * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.qv, qv, N * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.Tg, ground_T, NG * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.Pg, ground_p, NG * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.p, p3d, N * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaMemcpyAsync(e.gh, gh, NG * 4, cudaMemcpyHostToDevice, e.stream);
+    launch_init_state(e, (flags & SKT_INIT_NOISE) ? 1 : 0, noise_seed);
+    cudaStreamSynchronize(e.stream);
+    const skt_status st = cuda_check(e, "init");
+    if (st == SKT_OK) e.initialized = true;
+    return st;
+}
+
+skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (!e.initialized) return fail(&e, SKT_NOT_INITIALIZED, "skt_init has not run");
+    if (!(dt > 0.0f) || !(speed > 0.0f) || nsteps < 0) return fail(&e, SKT_INVALID_ARG, "dt and speed must be > 0, nsteps >= 0");
+    skt_status worst = SKT_OK;
+    if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
+    cudaEventRecord(e.ev0, e.stream);
+    for (int i = 0; i < nsteps; ++i) {
+        const skt_status st = run_step(e, dt, speed);
+        if (st != SKT_OK) return st;
+        if (!e.last_converged) worst = SKT_NOT_CONVERGED;
+    }
+    cudaEventRecord(e.ev1, e.stream);
+    cudaEventSynchronize(e.ev1);
+    cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
+    const skt_status st = cuda_check(e, "step");
+    return st != SKT_OK ? st : worst;
+}
+
+skt_status skt_sync(skt_env* env) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    cudaStreamSynchronize(env->e.stream);
+    return cuda_check(env->e, "sync");
+}
+
+skt_status skt_read_field(skt_env* env, int param, int dir, float* dst, size_t n) {
+    if (!env || !dst) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    float* src = sky_ptr(e, param, dir);
+    if (!src) return fail(&e, SKT_INVALID_ARG, "unknown field selector");
+    if (n != size_t(e.g.N)) return fail(&e, SKT_INVALID_ARG, "size mismatch");
+    cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "read_field");
+}
+
+skt_status skt_write_field(skt_env* env, int param, int dir, const float* src, size_t n) {
+    if (!env || !src) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    float* dst = sky_ptr(e, param, dir);
+    if (!dst) return fail(&e, SKT_INVALID_ARG, "unknown field selector");
+    if (n != size_t(e.g.N)) return fail(&e, SKT_INVALID_ARG, "size mismatch");
+    cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "write_field");
+}
+
+skt_status skt_field_device_ptr(skt_env* env, int param, int dir, float** out) {
+    if (!env || !out) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    float* p = sky_ptr(env->e, param, dir);
+    if (!p) return fail(&env->e, SKT_INVALID_ARG, "unknown field selector");
+    *out = p;
+    return SKT_OK;
+}
+
+skt_status skt_read_ground(skt_env* env, int which, float* dst, size_t n) {
+    if (!env || !dst) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    float* src = ground_ptr(e, which);
+    if (!src || n != size_t(e.g.X) * e.g.Z) return fail(&e, SKT_INVALID_ARG, "bad ground selector or size");
+    cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "read_ground");
+}
+
+skt_status skt_write_ground(skt_env* env, int which, const float* src, size_t n) {
+    if (!env || !src) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    float* dst = ground_ptr(e, which);
+    if (!dst || n != size_t(e.g.X) * e.g.Z) return fail(&e, SKT_INVALID_ARG, "bad ground selector or size");
+    cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "write_ground");
+}
+
+skt_status skt_read_column(skt_env* env, int which, float* dst, size_t n) {
+    if (!env || !dst) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    float* src = column_ptr(e, which);
+    if (!src || n != size_t(e.g.Y)) return fail(&e, SKT_INVALID_ARG, "bad column selector or size");
+    cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "read_column");
+}
+
+skt_status skt_write_column(skt_env* env, int which, const float* src, size_t n) {
+    if (!env || !src) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    float* dst = column_ptr(e, which);
+    if (!dst || n != size_t(e.g.Y)) return fail(&e, SKT_INVALID_ARG, "bad column selector or size");
+    cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyHostToDevice, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "write_column");
+}
+
+skt_status skt_set_clock(skt_env* env, double sim_time, int day, float longitude, float sun, int pause) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    e.sim_time = float(sim_time);
+    e.day = day;
+    e.longitude = longitude;
+    e.sun = sun;
+    e.pause = pause;
+    return SKT_OK;
+}
+
+skt_status skt_stats(skt_env* env, skt_step_stats* out) {
+    if (!env || !out) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    out->pcg_iters = e.last_iters;
+    out->pcg_residual = e.last_residual;
+    out->pcg_converged = e.last_converged;
+    for (int i = 0; i < 10; ++i) out->nsub[i] = e.last_nsub[i];
+    out->outer_iters = e.last_outer;
+    out->sim_time = e.sim_time;
+    out->kernel_launches = e.launches;
+    out->gpu_ms = e.last_gpu_ms;
+    return SKT_OK;
+}
+
+skt_status skt_profile_enable(skt_env* env, int on) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    env->e.prof = on != 0;
+    return SKT_OK;
+}
+
+skt_status skt_profile_read(skt_env* env, char* buf, size_t n) {
+    if (!env || !buf || n == 0) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    cudaStreamSynchronize(e.stream);
+    struct Acc { std::string name; double ms; long long nk; int scopes; };
+    std::vector<Acc> acc;
+    for (auto& r : e.recs) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+        size_t i = 0;
+        for (; i < acc.size(); ++i)
+            if (acc[i].name == r.name) break;
+        if (i == acc.size()) acc.push_back({r.name, 0.0, 0, 0});
+        acc[i].ms += ms;
+        acc[i].nk += r.nk;
+        acc[i].scopes += 1;
+    }
+    e.recs.clear();
+    std::string js = "{";
+    for (size_t i = 0; i < acc.size(); ++i) {
+        char tmp[256];
+        snprintf(tmp, sizeof tmp, "%s\"%s\": [%.6f, %lld, %d]", i ? ", " : "", acc[i].name.c_str(), acc[i].ms, acc[i].nk, acc[i].scopes);
+        js += tmp;
+    }
+    js += "}";
+    if (js.size() + 1 > n) return fail(&e, SKT_INVALID_ARG, "buffer too small");
+    memcpy(buf, js.c_str(), js.size() + 1);
+    return cuda_check(e, "profile_read");
+}
+
+skt_status skt_run_stage(skt_env* env, int stage, int arg, float dt, float speed, skt_step_stats* out) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (!e.initialized) return fail(&e, SKT_NOT_INITIALIZED, "skt_init has not run");
+    switch (stage) {
+        case 0: {
+            float* f[6] = {e.th, e.qv, e.u, e.v, e.w, e.qw};
+            if (arg < 0 || arg > 5) return fail(&e, SKT_INVALID_ARG, "diffuse type");
+            launch_diffuse(e, f[arg], arg, dt);
+            break;
+        }
+        case 1: {
+            if (arg < 0 || arg > 5) return fail(&e, SKT_INVALID_ARG, "advect field");
+            float* f[6] = {e.th, e.u, e.v, e.w, e.qv, e.qw};
+            const float* df[6] = {e.isenT, e.defU, e.zeroY, e.defW, e.isenQv, e.zeroY};
+            const int sd[6] = {CUSTOM, CUSTOM, DIRICHLET, CUSTOM, CUSTOM, DIRICHLET};
+            const int gd[6] = {CUSTOM, DIRICHLET, DIRICHLET, DIRICHLET, CUSTOM, DIRICHLET};
+            e.last_nsub[0] = launch_advect(e, f[arg], df[arg], sd[arg], gd[arg], dt, 0, true);
+            break;
+        }
+        case 2: launch_buoyancy(e, dt); break;
+        case 3: launch_init_density(e); launch_project(e, dt); break;
+        case 4: launch_micro(e, dt, speed); break;
+        case 5: {
+            if (arg < 0 || arg > 2) return fail(&e, SKT_INVALID_ARG, "precip type");
+            float* f[3] = {e.qr, e.qs, e.qi};
+            launch_precip(e, f[arg], arg, dt);
+            break;
+        }
+        case 6: launch_ground(e, dt, speed, irradiance(e.sim_time, e.day, e.longitude, e.sun)); break;
+        case 8: launch_init_density(e); break;
+        case 9: launch_new_pressure(e); break;
+        default: return fail(&e, SKT_INVALID_ARG, "unknown stage");
+    }
+    cudaStreamSynchronize(e.stream);
+    const skt_status st = cuda_check(e, "stage");
+    if (out) skt_stats(env, out);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// Internal declarations shared by the CUDA translation units of libskewt_gb300.
+//
+// Data layout in HBM: structure-of-arrays FP32 fields of X*Y*Z cells, idx = x + y*X + z*X*Y
+// with y vertical (the reference's layout, Game/utils.cuh:8-11); 2D ground arrays of X*Z
+// cells, idxG = x + z*X; per-level columns of Y values. A cell is ground when
+// y <= gh[x + z*X] (Game/kernelSky.cu:1709-1712). All fields live in one allocation carved into
+// 256-byte aligned slices.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "skt_physics.cuh"
+
+namespace skt {
+
+enum BC : int { NEUMANN = 0, DIRICHLET = 1, CUSTOM = 2 };
+
+struct Grid {
+    int X, Y, Z;  // Y vertical
+    int XY;       // X*Y
+    int N;        // X*Y*Z (< 2^31)
+    const int* __restrict__ gh;
+    float vox;
+};
+
+__device__ __forceinline__ int cidx(const Grid& g, int x, int y, int z) { return x + y * g.X + z * g.XY; }
+__device__ __forceinline__ bool is_ground(const Grid& g, int x, int y, int z) { return y <= __ldg(g.gh + x + z * g.X); }
+__device__ __forceinline__ bool in_dom(const Grid& g, int x, int y, int z) {
+    return (unsigned)x < (unsigned)g.X && (unsigned)y < (unsigned)g.Y && (unsigned)z < (unsigned)g.Z;
+}
+__device__ __forceinline__ float bc_val(int bc, float own, float custom) {
+    return bc == NEUMANN ? own : (bc == DIRICHLET ? 0.0f : custom);
+}
+
+// Value of field q seen by a sky-cell stencil at (x,y,z), which may be outside the domain or a
+// ground cell. Outside: the condition of the nearest in-domain cell ("ground" if that cell is
+// ground, else "sides"; the top boundary also uses "sides") with that cell's value and the
+// default column at its height. In-domain ground: the "ground" condition with the default at
+// that height. This one rule restates the reference's Neigh records plus fillNeighbourData,
+// fillSharedNeigh and getValueExtra* (Game/kernelSky.cu:1765-2042).
+__device__ __forceinline__ float ghost(const Grid& g, const float* __restrict__ q, int x, int y, int z, int sides, int ground,
+                                       const float* __restrict__ def) {
+    if (!in_dom(g, x, y, z)) {
+        const int xc = min(max(x, 0), g.X - 1), yc = min(max(y, 0), g.Y - 1), zc = min(max(z, 0), g.Z - 1);
+        const int bc = is_ground(g, xc, yc, zc) ? ground : sides;
+        return bc_val(bc, q[cidx(g, xc, yc, zc)], def ? def[yc] : 0.0f);
+    }
+    if (is_ground(g, x, y, z)) return bc_val(ground, q[cidx(g, x, y, z)], def ? def[y] : 0.0f);
+    return q[cidx(g, x, y, z)];
+}
+
+// Face value through fillNeighbourData with an explicit custom value (the velocity of the
+// face behind a cell and the boundary densities/pressures of the projection).
+__device__ __forceinline__ float face_nb(const Grid& g, const float* __restrict__ q, int x, int y, int z, int dx, int dy, int dz,
+                                         int sides, int ground, float custom) {
+    const int xn = x + dx, yn = y + dy, zn = z + dz;
+    const float own = q[cidx(g, x, y, z)];
+    if (!in_dom(g, xn, yn, zn)) return bc_val(sides, own, custom);
+    if (is_ground(g, xn, yn, zn)) return bc_val(ground, own, custom);
+    return q[cidx(g, xn, yn, zn)];
+}
+
+// Device-resident scalars of the solver (one per environment).
+struct Scalars {
+    double sigma0, sigma1, beta;      // PCG scalars (FP64)
+    float alpha, beta_f;              // the FP32 step lengths applied to the vectors
+    unsigned int maxbits;             // float bits of a max-reduction (atomicMax on uint)
+    int converged;                    // PCG stop flag
+    int iters;                        // PCG iterations done
+    float residual;                   // last max residual
+    unsigned int done_blocks;         // last-block reduction ticket
+    unsigned int done_blocks2;
+    int nsub;                         // Courant substeps of the current advection
+    int status;                       // 0 ok, otherwise an skt_status
+    double rnorm0;                    // mixed mode: initial residual norm
+    double rnorm;                     // mixed mode: current residual norm
+    int outer;                        // mixed mode: refinement steps
+    int pad;
+};
+
+constexpr int kMaxPartials = 4096;
+
+// Kernel-level configuration (from skt_solver_cfg)
+struct SolverCfg {
+    int semantics;       // 0 reference, 1 textbook
+    int diffuse_sweeps;
+    float pcg_tol;
+    int pcg_max_iter;
+    int max_substeps;
+    int precision;       // 0 plain, 1 mixed
+    float refine_tol;
+    int inner_max_iter;
+    float inner_rtol;
+    int use_graph;
+};
+
+struct Env {
+    Grid g{};
+    SolverCfg cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* pool = nullptr;
+    size_t pool_bytes = 0;
+    // sky fields
+    float *th, *qv, *qw, *qc, *qr, *qs, *qi, *u, *v, *w, *p, *rho;
+    // scratch sky fields
+    float *tA, *tB;               // ping-pong for diffusion/advection
+    float *r, *s, *As, *pp;       // PCG vectors
+    float *ax, *ay, *az, *aw;     // Poisson coefficients (+x, +y, +z faces, diagonal)
+    double *xd, *rd;              // mixed mode FP64 solution and residual
+    // ground (X*Z)
+    float *Qrs, *Qgr, *Qgs, *Qgi, *Pg, *tg, *Tg, *cover, *g2a, *g2b;
+    int* gh;
+    // columns (Y)
+    float *isenT, *isenQv, *defU, *defW, *zeroY;
+    // reductions
+    Scalars* sc;
+    double* partials;
+    float* host_scalars;  // pinned
+    Scalars* host_sc;     // pinned mirror
+    // host clock (environmentGPU::m_time etc.)
+    float sim_time = 43200.0f;
+    int day = 130;
+    float longitude = 52.37f;
+    float sun = 1.0f;
+    int pause = 0;
+    bool initialized = false;
+    Gammas gam{};
+    // last-step diagnostics
+    int last_iters = 0;
+    float last_residual = 0.0f;
+    int last_converged = 1;
+    int last_nsub[10] = {0};
+    int last_outer = 0;
+    int num_sms = 148;
+    std::string err;
+    int flat = 1;  // all gh == 0
+    // graph
+    cudaGraphExec_t graph_exec = nullptr;
+    float graph_dt = 0.0f, graph_speed = 0.0f;
+    // launch accounting and optional per-stage event timing
+    long long launches = 0;
+    float last_gpu_ms = 0.0f;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool prof = false;
+    struct ProfRec { const char* name; cudaEvent_t a, b; int nk; };
+    std::vector<ProfRec> recs;
+};
+
+// Times the kernels queued between construction and destruction when profiling is on.
+struct ProfScope {
+    Env& e;
+    const char* name;
+    cudaEvent_t a = nullptr;
+    long long l0;
+    ProfScope(Env& env, const char* n) : e(env), name(n), l0(env.launches) {
+        if (e.prof) { cudaEventCreate(&a); cudaEventRecord(a, e.stream); }
+    }
+    ~ProfScope() {
+        if (e.prof) {
+            cudaEvent_t b;
+            cudaEventCreate(&b);
+            cudaEventRecord(b, e.stream);
+            e.recs.push_back({name, a, b, int(e.launches - l0)});
+        }
+    }
+};
+
+// ---- launchers (defined in the kernel translation units) --------------------------------------
+void launch_diffuse(Env& e, float* f, int type, float dtS);
+int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int field_slot, bool host_sync);
+void launch_precip(Env& e, float* q, int type, float dtS);
+void launch_buoyancy(Env& e, float dtS);
+void launch_init_density(Env& e);
+void launch_new_pressure(Env& e);
+void launch_project(Env& e, float dtS);
+void launch_micro(Env& e, float dt, float speed);
+void launch_ground(Env& e, float dt, float speed, float irr);
+void launch_init_state(Env& e, int noise, uint32_t seed);
+
+}  // namespace skt

@@ -1,0 +1,439 @@
+// Stencil kernels of the atmosphere step: diffusion, PPM advection, Courant max, sedimentation,
+// buoyancy and the equation of state.
+#include "skt_internal.cuh"
+
+namespace skt {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+inline dim3 cell_grid(const Grid& g) { return dim3((g.X + BX - 1) / BX, (g.Y + BY - 1) / BY, g.Z); }
+
+// theta at a ground face seen from cell idx: potentialTempGPU(Tg-273.15, p_cell, Pg)+273.15
+// (Game/kernelSky.cu:95-100)
+__device__ __forceinline__ float theta_ground(const float* p, const float* Tg, const float* Pg, int idx, int idxg) {
+    return potentialTemp(Tg[idxg] - 273.15f, p[idx], Pg[idxg]) + 273.15f;
+}
+
+// One Jacobi sweep of the colour-split diffusion (diffuseRedBlack Game/kernelSky.cu:43-115; both
+// colours read the same input array, Game/environment.cu:651-662).
+template <bool THETA>
+__global__ void __launch_bounds__(256) k_diffuse(Grid g, const float* __restrict__ in, float* __restrict__ out, int sides, int ground,
+                                                 const float* __restrict__ def, float k, const float* __restrict__ p,
+                                                 const float* __restrict__ Tg, const float* __restrict__ Pg) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= g.X || y >= g.Y) return;
+    if (is_ground(g, x, y, z)) return;
+    const int c = cidx(g, x, y, z);
+    float l = ghost(g, in, x - 1, y, z, sides, ground, def);
+    float r = ghost(g, in, x + 1, y, z, sides, ground, def);
+    float d = ghost(g, in, x, y - 1, z, sides, ground, def);
+    float u = ghost(g, in, x, y + 1, z, sides, ground, def);
+    float f = ghost(g, in, x, y, z + 1, sides, ground, def);
+    float b = ghost(g, in, x, y, z - 1, sides, ground, def);
+    if (THETA) {
+        const int idxG = x + z * g.X;
+        if (y > 0 && is_ground(g, x, y - 1, z)) d = theta_ground(p, Tg, Pg, c, idxG);
+        // lateral ground faces: only when isGroundLevel(z) holds for the reference's 16-wide tile
+        // launch (Q5, Game/kernelSky.cu:1684-1694): blockIdx.x == GHeight[threadIdx.x + z*Z] + 1
+        const bool gl = x > 0 && is_ground(g, x - 1, y, z), gr = x + 1 < g.X && is_ground(g, x + 1, y, z);
+        const bool gf = z + 1 < g.Z && is_ground(g, x, y, z + 1), gb = z > 0 && is_ground(g, x, y, z - 1);
+        if (gl | gr | gf | gb) {
+            const int bw = min(16, g.X);
+            int gi = (x % bw) + z * g.Z;
+            if (gi >= g.X * g.Z) gi = g.X * g.Z - 1;
+            const bool level = (x / bw) == g.gh[gi] + 1;
+            if (level) {
+                const int idxGL = x > 0 ? idxG - 1 : idxG, idxGR = x + 1 < g.X ? idxG + 1 : idxG;
+                const int idxGF = z + g.X < g.Z ? idxG + g.X : idxG;  // the reference compares z + X < Z
+                const int idxGB = z > 0 ? idxG - g.X : idxG;
+                if (gl) l = theta_ground(p, Tg, Pg, c, idxGL);
+                if (gr) r = theta_ground(p, Tg, Pg, c, idxGR);
+                if (gf) f = theta_ground(p, Tg, Pg, c, idxGF);
+                if (gb) b = theta_ground(p, Tg, Pg, c, idxGB);
+            }
+        }
+    }
+    out[c] = (in[c] + k * (l + r + u + d + f + b)) / (1 + 6 * k);
+}
+
+// advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp)
+__device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float vR, float dt, float vox) {
+    float C = veli * dt / vox;
+    C = C > 1.0f ? 1.0f : (C < -1.0f ? -1.0f : C);
+    const float qMin = fminf(vL, fminf(vC, vR));
+    const float qMax = fmaxf(vL, fmaxf(vC, vR));
+    float s = 0.0f;
+    const float dl = vC - vL, dr = vR - vC;
+    if (dl * dr > 0.0f) {
+        const float db = vR - vL;
+        const float lim = fminf(0.5f * fabsf(db), fminf(fabsf(dr), fabsf(dl)));
+        s = db >= 0.0f ? lim : -lim;
+    }
+    const float qLS = vC - 0.5f * s, qRS = vC + 0.5f * s;
+    float B = 1.0f;
+    if (qRS > qMax) { const float den = qRS - vC; if (den > 1e-16f) B = fminf(B, (qMax - vC) / den); }
+    if (qLS < qMin) { const float den = vC - qLS; if (den > 1e-16f) B = fminf(B, (vC - qMin) / den); }
+    float qR = vC + B * (qRS - vC);
+    float qL = vC + B * (qLS - vC);
+    if ((qR - vC) * (vC - qL) <= 0.0f) { qR = qL = vC; }
+    float qq;
+    if (C > 0.0f) qq = qR + C * (-qL - 2 * qR + 3 * vC) + C * C * (qL + qR - 2 * vC);
+    else qq = qR + C * (-2 * qL - qR + 3 * vC) + C * C * (qL + qR - 2 * vC);
+    return veli * qq;
+}
+
+// ghost value of the density companion (a field of ones, custom value 1)
+__device__ __forceinline__ float ghost_one(const Grid& g, int x, int y, int z, int sides, int ground) {
+    if (!in_dom(g, x, y, z)) {
+        const int xc = min(max(x, 0), g.X - 1), yc = min(max(y, 0), g.Y - 1), zc = min(max(z, 0), g.Z - 1);
+        return bc_val(is_ground(g, xc, yc, zc) ? ground : sides, 1.0f, 1.0f);
+    }
+    if (is_ground(g, x, y, z)) return bc_val(ground, 1.0f, 1.0f);
+    return 1.0f;
+}
+
+// One directional PPM pass (advectPPMX/Y/Z Game/kernelSky.cu:368-574) of q and of the density
+// companion (advected ones), followed by q/rho* (divideValues Game/kernelMaths.cu:38).
+// The velocity array is read as it stands when the pass starts.
+template <int AXIS>
+__global__ void __launch_bounds__(256) k_ppm(Grid g, const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ vel,
+                                             const float* __restrict__ def, int sides, int ground, const float* __restrict__ defU,
+                                             const float* __restrict__ defW, float dtFull, int nsub_host, int half,
+                                             const Scalars* __restrict__ sc, int slot) {
+    int nsub = nsub_host;
+    if (sc) {
+        nsub = sc->nsub;
+        if (slot >= nsub) return;
+    }
+    const float dtSub = dtFull / float(nsub);
+    const float dt = half ? dtSub * 0.5f : dtSub;
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= g.X || y >= g.Y) return;
+    if (is_ground(g, x, y, z)) return;
+    constexpr int ax = AXIS == 0, ay = AXIS == 1, az = AXIS == 2;
+    const int c = cidx(g, x, y, z);
+    const float vox = g.vox;
+    float q[5], o[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const int off = i - 2;
+        if (off == 0) { q[i] = in[c]; o[i] = 1.0f; continue; }
+        q[i] = ghost(g, in, x + off * ax, y + off * ay, z + off * az, sides, ground, def);
+        o[i] = ghost_one(g, x + off * ax, y + off * ay, z + off * az, sides, ground);
+    }
+    const float custom = AXIS == 0 ? defU[y] : (AXIS == 1 ? 0.0f : defW[y]);
+    const float vc = vel[c];
+    const float vm = face_nb(g, vel, x, y, z, -ax, -ay, -az, sides, ground, custom);
+    float nq, nr;
+    {
+        float L, C, R;
+        if (vc >= 0.0f) { L = q[1]; C = q[2]; R = q[3]; } else { L = q[4]; C = q[3]; R = q[2]; }
+        const float fp = ppm_flux(vc, L, C, R, dt, vox);
+        if (vm < 0.0f) { L = q[3]; C = q[2]; R = q[1]; } else { L = q[0]; C = q[1]; R = q[2]; }
+        const float fm = ppm_flux(vm, L, C, R, dt, vox);
+        nq = in[c] - (dt / vox) * (fp - fm);
+    }
+    {
+        float L, C, R;
+        if (vc >= 0.0f) { L = o[1]; C = o[2]; R = o[3]; } else { L = o[4]; C = o[3]; R = o[2]; }
+        const float fp = ppm_flux(vc, L, C, R, dt, vox);
+        if (vm < 0.0f) { L = o[3]; C = o[2]; R = o[1]; } else { L = o[0]; C = o[1]; R = o[2]; }
+        const float fm = ppm_flux(vm, L, C, R, dt, vox);
+        nr = 1.0f - (dt / vox) * (fp - fm);
+    }
+    out[c] = nq / nr;
+}
+
+// copy the sky cells of src into dst (the end-of-substep copy, Game/environment.cu:805)
+__global__ void __launch_bounds__(256) k_copy_sky(Grid g, const float* __restrict__ src, float* __restrict__ dst, const Scalars* __restrict__ sc, int slot) {
+    if (sc && slot >= sc->nsub) return;
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= g.X || y >= g.Y) return;
+    if (is_ground(g, x, y, z)) return;
+    const int c = cidx(g, x, y, z);
+    dst[c] = src[c];
+}
+
+// Max over sky cells of three fields (getMaxDivergence Game/kernelSky.cu:910-953 applied to
+// u, v and w into one slot). reference=1: |a| at z=0, signed a for z>=1, floored at 0.
+__global__ void __launch_bounds__(256) k_maxvel(Grid g, const float* __restrict__ a0, const float* __restrict__ a1, const float* __restrict__ a2,
+                                                int reference, Scalars* __restrict__ sc) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    float m = 0.0f;
+    if (x < g.X && y < g.Y && !is_ground(g, x, y, z)) {
+        const int c = cidx(g, x, y, z);
+        const bool absv = !reference || z == 0;
+        float v0 = a0[c], v1 = a1[c], v2 = a2[c];
+        if (absv) { v0 = fabsf(v0); v1 = fabsf(v1); v2 = fabsf(v2); }
+        if (v0 > m) m = v0;
+        if (v1 > m) m = v1;
+        if (v2 > m) m = v2;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float t = __shfl_xor_sync(0xffffffffu, m, o);
+        if (t > m) m = t;
+    }
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(&sc->maxbits, __float_as_uint(m));
+}
+
+// Courant substeps from the max velocity, on the device (Game/environment.cu:726-730)
+__global__ void k_nsub(Scalars* sc, float dt, float vox, float maxsub) {
+    const float maxVel = __uint_as_float(sc->maxbits);
+    const float C = maxVel * dt / vox;
+    sc->nsub = int(fminf(ceilf(fabsf(C)), maxsub));
+}
+
+// Sedimentation of one precipitation species (advectPrecipGPU Game/kernelSky.cu:576-657), one
+// thread per (x,z) column marching up; each cell loses its outflow and gains the outflow of the
+// cell above, both from the values at the start of the substep.
+__global__ void __launch_bounds__(128) k_precip(Grid g, float* __restrict__ q, const float* __restrict__ th, const float* __restrict__ qv,
+                                                const float* __restrict__ p, const float* __restrict__ Pg, int type, float dt, Gammas G) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.X * g.Z) return;
+    const int x = col % g.X, z = col / g.X;
+    const int gh = g.gh[col];
+    const float vox = g.vox;
+    const float pgc = Pg[col];
+    auto fall = [&](float Q, int i) {
+        const float T = th[i] * powf(p[i] / pgc, KC::KAPPA);
+        const float Tv = T * (0.608f * qv[i] + 1);
+        const float dens = p[i] * 100 / (KC::Rsd * Tv);
+        float UR, US, UI;
+        fallingVelocity(Q, Q, Q, dens, type, G.Qr, G.Qs, G.Qi, UR, US, UI);
+        return type == 0 ? UR : (type == 1 ? US : UI);
+    };
+    int y = max(gh + 1, 0);
+    if (y >= g.Y) return;
+    int c = cidx(g, x, y, z);
+    float QC = q[c];
+    float fv = fall(QC, c);
+    for (; y < g.Y; ++y) {
+        const bool up = y < g.Y - 1;
+        float QU = 0.0f, fvu = 0.0f;
+        if (up) { QU = q[c + g.X]; fvu = fall(QU, c + g.X); }
+        float val = QC;
+        val -= dt * fminf((fv / vox) * QC, QC);
+        if (up) val += dt * fminf((fvu / vox) * QU, QU);
+        q[c] = val;
+        QC = QU;
+        fv = fvu;
+        c += g.X;
+    }
+}
+
+// buoyancyGPU Game/kernelSky.cu:1061-1247 (bounds DIRICHLET everywhere)
+__global__ void __launch_bounds__(256) k_buoyancy(Grid g, float* __restrict__ v, const float* __restrict__ th, const float* __restrict__ qv,
+                                                  const float* __restrict__ qr, const float* __restrict__ qs, const float* __restrict__ qi,
+                                                  const float* __restrict__ isenT, const float* __restrict__ isenQv,
+                                                  const float* __restrict__ p, const float* __restrict__ Pg, float dt) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= g.X || y >= g.Y) return;
+    if (is_ground(g, x, y, z)) return;
+    const int c = cidx(g, x, y, z);
+    const float vel = v[c];
+    const bool up = y < g.Y - 1;
+    const bool down = y > 0 && !is_ground(g, x, y - 1, z);
+    auto valid = [&](int dx, int dz) { return in_dom(g, x + dx, y, z + dz) && !is_ground(g, x + dx, y, z + dz); };
+    const int nv = int(valid(-1, 0)) + int(valid(1, 0)) + int(valid(0, -1)) + int(valid(0, 1));
+    if (nv == 0) return;
+    const float Pgs = Pg[x + z * g.X];
+    const float psC = p[c];
+    const float psU = up ? p[c + g.X] : psC;
+    const float psD = down ? p[c - g.X] : psC;
+    auto Q = [&](int dx, int dy, int dz) { return ghost(g, qv, x + dx, y + dy, z + dz, DIRICHLET, DIRICHLET, isenQv); };
+    auto TH = [&](int dx, int dy, int dz) { return ghost(g, th, x + dx, y + dy, z + dz, DIRICHLET, DIRICHLET, isenT); };
+    const float QP = qv[c];
+    const float Qenv = (Q(1, 0, 0) + Q(-1, 0, 0) + Q(0, 0, 1) + Q(0, 0, -1)) / nv;
+    const float QenvUp = Q(0, 1, 0), QenvDown = Q(0, -1, 0);
+    const float thc = th[c];
+    const float thU = TH(0, 1, 0), thD = TH(0, -1, 0);
+    const float TDown = thD * powf(psD / Pgs, KC::KAPPA);
+    const float Tc = thc * powf(psC / Pgs, KC::KAPPA);
+    const float TUp = thU * powf(psU / Pgs, KC::KAPPA);
+    float Tad = thc, TadUp = thc, TadDown = thc;
+    const float Tenv = (TH(1, 0, 0) + TH(-1, 0, 0) + TH(0, 0, 1) + TH(0, 0, -1)) / nv;
+    const float TenvUp = thU, TenvDown = thD;
+    if (down) {
+        if ((Tc < 0.0f && QP >= wi(TDown - 273.15f, psD)) || QP >= ws(TDown - 273.15f, psD)) {
+            TadDown = Tc - MLR(Tc - 273.15f, psC) * (psC - psD);
+            TadDown = TadDown * powf(Pgs / psD, KC::KAPPA);
+        }
+    }
+    if (up) {
+        if ((Tc < 0.0f && QP >= wi(TUp - 273.15f, psU)) || QP >= ws(TUp - 273.15f, psU)) {
+            TadUp = MLR(Tc - 273.15f, psC) * (psU - psC) + Tc;
+            TadUp = TadUp * powf(Pgs / psU, KC::KAPPA);
+        }
+    }
+    float B = 0.0f, BUp = 0.0f, BDown = 0.0f;
+    const float totalQ = qr[c] + qs[c] + qi[c];
+    if (down) {
+        const float VTP = TadDown * (1.0f + 0.608f * QP), VTE = TenvDown * (1.0f + 0.608f * QenvDown);
+        BDown = KC::g * ((VTP - VTE) / VTE) - totalQ * KC::g;
+    }
+    {
+        const float VTP = Tad * (1.0f + 0.608f * QP), VTE = Tenv * (1.0f + 0.608f * Qenv);
+        B = KC::g * ((VTP - VTE) / VTE) - totalQ * KC::g;
+    }
+    if (up) {
+        const float VTP = TadUp * (1.0f + 0.608f * QP), VTE = TenvUp * (1.0f + 0.608f * QenvUp);
+        BUp = KC::g * ((VTP - VTE) / VTE) - totalQ * KC::g;
+    }
+    float fin = B;
+    if (vel > 0.0f) fin = BUp;
+    else if (vel < 0.0f) fin = BDown;
+    float change = fin * dt;
+    if ((up && vel > 0.0f && -change > vel) || (down && vel < 0.0f && -change < vel)) change = -vel;
+    v[c] = vel + change;
+}
+
+// initDensity Game/kernelSky.cu:1432-1452
+__global__ void __launch_bounds__(256) k_init_density(Grid g, float* __restrict__ rho, const float* __restrict__ th, const float* __restrict__ p,
+                                                      const float* __restrict__ qv, const float* __restrict__ Pg) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= g.X || y >= g.Y) return;
+    if (is_ground(g, x, y, z)) return;
+    const int c = cidx(g, x, y, z);
+    const float T = th[c] * powf(p[c] / Pg[x + z * g.X], KC::KAPPA);
+    const float Tv = T * (0.608f * qv[c] + 1);
+    rho[c] = p[c] * 100 / (KC::Rsd * Tv);
+}
+
+// calculateNewPressure Game/kernelSky.cu:1454-1474
+__global__ void __launch_bounds__(256) k_new_pressure(Grid g, float* __restrict__ p, const float* __restrict__ rho, const float* __restrict__ th,
+                                                      const float* __restrict__ qv, const float* __restrict__ Pg) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= g.X || y >= g.Y) return;
+    if (is_ground(g, x, y, z)) return;
+    const int c = cidx(g, x, y, z);
+    const float T = th[c] * powf(p[c] / Pg[x + z * g.X], KC::KAPPA);
+    const float Tv = T * (0.608f * qv[c] + 1);
+    p[c] = rho[c] * KC::Rsd * Tv / 100.0f;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------------------
+
+// diffuseGPU Game/environment.cu:597-673: per-type boundary table :603-638, k = 0.005*dt/vox^2
+void launch_diffuse(Env& e, float* f, int type, float dtS) {
+    const Grid& g = e.g;
+    const float* def = nullptr;
+    int sides = NEUMANN, ground = DIRICHLET;
+    switch (type) {
+        case 0: def = e.isenT; sides = CUSTOM; ground = CUSTOM; break;
+        case 1: def = e.isenQv; sides = CUSTOM; ground = DIRICHLET; break;
+        case 2: def = e.defU; sides = CUSTOM; break;
+        case 3: def = nullptr; sides = NEUMANN; break;
+        case 4: def = e.defW; sides = CUSTOM; break;
+        default: def = e.zeroY; break;
+    }
+    const float k = 0.005f * dtS / (g.vox * g.vox);
+    const int sweeps = e.cfg.diffuse_sweeps;
+    ProfScope ps(e, "diffuse");
+    e.launches += sweeps + 1;
+    cudaMemcpyAsync(e.tA, f, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
+    cudaMemcpyAsync(e.tB, f, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
+    float* a = e.tA;
+    float* o = e.tB;
+    for (int s = 0; s < sweeps; ++s) {
+        const float* in = (s % 2 == 0) ? a : o;
+        float* out = (s % 2 == 0) ? o : a;
+        if (type == 0)
+            k_diffuse<true><<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
+        else
+            k_diffuse<false><<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
+    }
+    const float* res = (sweeps % 2 == 0) ? a : o;
+    k_copy_sky<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, res, f, nullptr, 0);
+}
+
+// advectPPMWGPU Game/environment.cu:692-824. With host_sync the substep count is read back as
+// the reference does; otherwise max_substeps slots are launched and the ones beyond the device
+// count exit at once (graph capture). Returns the substep count (or -1 when not read back).
+int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int slot_id, bool host_sync) {
+    const Grid& g = e.g;
+    ProfScope ps(e, "advect");
+    e.launches += 2;
+    cudaMemsetAsync(&e.sc->maxbits, 0, sizeof(unsigned int), e.stream);
+    k_maxvel<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, e.u, e.v, e.w, e.cfg.semantics == 0, e.sc);
+    k_nsub<<<1, 1, 0, e.stream>>>(e.sc, dtS, g.vox, float(e.cfg.max_substeps));
+    int nsub = -1;
+    int slots;
+    const Scalars* chk = nullptr;
+    if (host_sync) {
+        cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
+        cudaStreamSynchronize(e.stream);
+        nsub = e.host_sc->nsub;
+        slots = nsub;
+    } else {
+        slots = e.cfg.max_substeps;
+        chk = e.sc;
+    }
+    const dim3 grd = cell_grid(g), blk(BX, BY);
+    float* A = f;
+    float* O = e.tA;
+    e.launches += 6LL * slots;
+    for (int i = 0; i < slots; ++i) {
+        // pass 1: X half, A -> O (velocity u as it stands: for f == u this is A)
+        k_ppm<0><<<grd, blk, 0, e.stream>>>(g, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+        // pass 2: Y half, O -> A; the velocity is v as it stands before the pass (for f == v: q0)
+        const float* vy = e.v;
+        if (f == e.v) {
+            cudaMemcpyAsync(e.tB, e.v, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
+            vy = e.tB;
+        }
+        k_ppm<1><<<grd, blk, 0, e.stream>>>(g, O, A, vy, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+        // pass 3: Z full, A -> O
+        k_ppm<2><<<grd, blk, 0, e.stream>>>(g, A, O, e.w, def, sides, ground, e.defU, e.defW, dtS, nsub, 0, chk, i);
+        // pass 4: Y half, O -> A
+        vy = e.v;
+        if (f == e.v) {
+            cudaMemcpyAsync(e.tB, e.v, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
+            vy = e.tB;
+        }
+        k_ppm<1><<<grd, blk, 0, e.stream>>>(g, O, A, vy, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+        // pass 5: X half, A -> O, then A = O on sky cells
+        k_ppm<0><<<grd, blk, 0, e.stream>>>(g, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+        k_copy_sky<<<grd, blk, 0, e.stream>>>(g, O, A, chk, i);
+    }
+    (void)slot_id;
+    return nsub;
+}
+
+// advectPrecip Game/environment.cu:826-849: substeps from the guessed fall speeds 5/1/8 m/s
+void launch_precip(Env& e, float* q, int type, float dtS) {
+    const Grid& g = e.g;
+    const float maxVel = type == 0 ? 5.0f : (type == 1 ? 1.0f : 8.0f);
+    const float C = maxVel * dtS / g.vox;
+    const int sub = int(fminf(ceilf(fabsf(C)), float(e.cfg.max_substeps)));
+    const float dts = dtS / float(sub);
+    const int cols = g.X * g.Z;
+    ProfScope ps(e, "precip");
+    e.launches += sub;
+    for (int i = 0; i < sub; ++i)
+        k_precip<<<(cols + 127) / 128, 128, 0, e.stream>>>(g, q, e.th, e.qv, e.p, e.Pg, type, dts, e.gam);
+}
+
+void launch_buoyancy(Env& e, float dtS) {
+    ProfScope ps(e, "buoyancy");
+    e.launches += 1;
+    k_buoyancy<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.isenT, e.isenQv, e.p, e.Pg, dtS);
+}
+void launch_init_density(Env& e) {
+    ProfScope ps(e, "eos");
+    e.launches += 1;
+    k_init_density<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.rho, e.th, e.p, e.qv, e.Pg);
+}
+void launch_new_pressure(Env& e) {
+    ProfScope ps(e, "eos");
+    e.launches += 1;
+    k_new_pressure<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.p, e.rho, e.th, e.qv, e.Pg);
+}
+
+}  // namespace skt

@@ -1,0 +1,242 @@
+"""Python mirror of the reference's ``environmentGPU`` (Game/environment.cuh:9-183).
+
+Same operations, names and argument meaning as the reference class: ``init`` takes the host
+arrays of environmentGPU::init (Game/environment.cu:249), ``update_gpu(dt, speed)`` is
+environmentGPU::updateGPU (:391), ``get_param_array(parameter, direction)`` returns the device
+pointer of a field (:1076). Field readback, which the reference does every step through
+editor::GPUSetEnv (Game/editor.cpp:226-260), is explicit here (``read``). Every call goes
+through the C ABI of libskewt_gb300; errors raise ``SktError`` carrying the skt_status.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from enum import IntEnum
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+
+
+class Status(IntEnum):
+    OK = 0
+    INVALID_ARG = 1
+    CUDA_ERROR = 2
+    NOT_CONVERGED = 3
+    NAN_DETECTED = 4
+    TIMEOUT = 5
+    OUT_OF_MEMORY = 6
+    NOT_INITIALIZED = 7
+    COURANT_LIMIT = 8
+
+
+class Parameter(IntEnum):  # Game/config.h:62-65
+    POTTEMP = 0
+    QV = 1
+    QW = 2
+    QC = 3
+    QR = 4
+    QS = 5
+    QI = 6
+    WIND = 7
+    PGROUND = 8
+    PRESSURE = 9
+    DENSITY = 100
+
+
+class Direction(IntEnum):  # Game/config.h:36-39
+    LEFT = 0
+    RIGHT = 1
+    UP = 2
+    DOWN = 3
+    FORWARD = 4
+    BACKWARD = 5
+
+
+class Ground(IntEnum):
+    QRS = 0
+    QGR = 1
+    QGS = 2
+    QGI = 3
+    P = 4
+    TIME_WET = 5
+    T = 6
+    CLOUD_COVER = 7
+
+
+class Column(IntEnum):
+    ISEN_T = 0
+    ISEN_QV = 1
+    DEF_U = 2
+    DEF_W = 3
+
+
+class SktError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{Status(status).name}: {msg}")
+        self.status = Status(status)
+
+
+# name -> (parameter, direction) for read/write
+FIELDS = {
+    "th": (Parameter.POTTEMP, 0), "qv": (Parameter.QV, 0), "qw": (Parameter.QW, 0), "qc": (Parameter.QC, 0),
+    "qr": (Parameter.QR, 0), "qs": (Parameter.QS, 0), "qi": (Parameter.QI, 0),
+    "u": (Parameter.WIND, Direction.RIGHT), "v": (Parameter.WIND, Direction.UP), "w": (Parameter.WIND, Direction.FORWARD),
+    "p": (Parameter.PRESSURE, 0), "rho": (Parameter.DENSITY, 0),
+}
+GROUND_FIELDS = {"Qrs": Ground.QRS, "Qgr": Ground.QGR, "Qgs": Ground.QGS, "Qgi": Ground.QGI, "Pg": Ground.P,
+                 "tg": Ground.TIME_WET, "Tg": Ground.T, "cover": Ground.CLOUD_COVER}
+COLUMNS = {"isenT": Column.ISEN_T, "isenQv": Column.ISEN_QV, "defU": Column.DEF_U, "defW": Column.DEF_W}
+
+
+@dataclass
+class SolverConfig:
+    semantics: int = 0          # 0 reference quirks, 1 textbook
+    diffuse_sweeps: int = 20
+    pcg_tol: float = 1e-5
+    pcg_max_iter: int = 200
+    max_substeps: int = 100
+    precision: int = 0          # 0 plain, 1 mixed
+    refine_tol: float = 1e-8
+    inner_max_iter: int = 60
+    inner_rtol: float = 1e-3
+    use_graph: int = 0
+
+    def c(self):
+        return _lib.SolverCfg(self.semantics, self.diffuse_sweeps, self.pcg_tol, self.pcg_max_iter, self.max_substeps,
+                              self.precision, self.refine_tol, self.inner_max_iter, self.inner_rtol, self.use_graph)
+
+
+def _fp(a):
+    return a.ctypes.data_as(_lib.c_float_p)
+
+
+class Environment:
+    """One simulated atmosphere on the current CUDA device."""
+
+    def __init__(self, nx: int, ny: int, nz: int, voxel: float, cfg: Optional[SolverConfig] = None):
+        self._L = _lib.load()
+        self.nx, self.ny, self.nz, self.voxel = nx, ny, nz, float(voxel)
+        self.n = nx * ny * nz
+        self.ng = nx * nz
+        self.cfg = cfg or SolverConfig()
+        g = _lib.GridDesc(nx, ny, nz, self.voxel)
+        c = self.cfg.c()
+        h = ctypes.c_void_p()
+        st = self._L.skt_create(ctypes.byref(g), ctypes.byref(c), ctypes.byref(h))
+        if st != 0:
+            raise SktError(st, self._L.skt_last_error(None).decode())
+        self._h = h
+
+    # -- lifetime --------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.skt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, allow=()):
+        if st != 0 and st not in allow:
+            raise SktError(st, self._L.skt_last_error(self._h).decode())
+        return Status(st)
+
+    # -- environmentGPU API ----------------------------------------------------------------
+    def init(self, theta, vel_aos, qv, ground_T, ground_p, p3d, p_column, ground_height, noise=True, noise_seed=100):
+        """environmentGPU::init (Game/environment.cu:249-389)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (theta, vel_aos, qv, ground_T, ground_p, p3d, p_column)]
+        gh = np.ascontiguousarray(ground_height, np.int32)
+        self._gh = gh.copy()
+        st = self._L.skt_init(self._h, *[_fp(a) for a in arrs], gh.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                              1 if noise else 0, noise_seed)
+        self._check(st)
+
+    def init_from(self, state, noise=True, noise_seed=100):
+        """init() from a ``sounding.InitialState``."""
+        self.init(state.theta, state.vel, state.qv, state.ground_T, state.ground_p, state.p3d, state.p_column,
+                  state.ground_height, noise=noise, noise_seed=noise_seed)
+
+    def update_gpu(self, dt: float, speed: float = 1.0, nsteps: int = 1) -> Status:
+        """environmentGPU::updateGPU (Game/environment.cu:391-555); NOT_CONVERGED is returned, not raised."""
+        return self._check(self._L.skt_step(self._h, dt, speed, nsteps), allow=(Status.NOT_CONVERGED,))
+
+    def sync(self):
+        self._check(self._L.skt_sync(self._h))
+
+    def get_param_array(self, parameter: int, direction: int = Direction.RIGHT) -> int:
+        """environmentGPU::getParamArray: device address of the field (int)."""
+        p = _lib.c_float_p()
+        self._check(self._L.skt_field_device_ptr(self._h, int(parameter), int(direction), ctypes.byref(p)))
+        return ctypes.cast(p, ctypes.c_void_p).value
+
+    # -- readback / injection --------------------------------------------------------------
+    def read(self, name: str) -> np.ndarray:
+        if name in FIELDS:
+            prm, d = FIELDS[name]
+            out = np.empty(self.n, np.float32)
+            self._check(self._L.skt_read_field(self._h, int(prm), int(d), _fp(out), out.size))
+        elif name in GROUND_FIELDS:
+            out = np.empty(self.ng, np.float32)
+            self._check(self._L.skt_read_ground(self._h, int(GROUND_FIELDS[name]), _fp(out), out.size))
+        elif name in COLUMNS:
+            out = np.empty(self.ny, np.float32)
+            self._check(self._L.skt_read_column(self._h, int(COLUMNS[name]), _fp(out), out.size))
+        else:
+            raise KeyError(name)
+        return out
+
+    def write(self, name: str, a):
+        a = np.ascontiguousarray(a, np.float32)
+        if name in FIELDS:
+            prm, d = FIELDS[name]
+            self._check(self._L.skt_write_field(self._h, int(prm), int(d), _fp(a), a.size))
+        elif name in GROUND_FIELDS:
+            self._check(self._L.skt_write_ground(self._h, int(GROUND_FIELDS[name]), _fp(a), a.size))
+        elif name in COLUMNS:
+            self._check(self._L.skt_write_column(self._h, int(COLUMNS[name]), _fp(a), a.size))
+        else:
+            raise KeyError(name)
+
+    def set_clock(self, sim_time=43200.0, day=130, longitude=52.37, sun=1.0, pause=0):
+        self._check(self._L.skt_set_clock(self._h, sim_time, day, longitude, sun, pause))
+
+    def stats(self) -> dict:
+        s = _lib.StepStats()
+        self._check(self._L.skt_stats(self._h, ctypes.byref(s)))
+        return {"pcg_iters": s.pcg_iters, "pcg_residual": s.pcg_residual, "converged": bool(s.pcg_converged),
+                "nsub": list(s.nsub), "outer_iters": s.outer_iters, "sim_time": s.sim_time,
+                "kernel_launches": s.kernel_launches, "gpu_ms": s.gpu_ms}
+
+    def profile(self, on: bool = True):
+        self._check(self._L.skt_profile_enable(self._h, 1 if on else 0))
+
+    def profile_read(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._L.skt_profile_read(self._h, buf, len(buf)))
+        return {k: {"ms": v[0], "kernels": v[1], "scopes": v[2]} for k, v in json.loads(buf.value.decode()).items()}
+
+    def run_stage(self, stage: int, arg: int = 0, dt: float = 0.5, speed: float = 1.0) -> dict:
+        s = _lib.StepStats()
+        self._check(self._L.skt_run_stage(self._h, stage, arg, dt, speed, ctypes.byref(s)))
+        return {"pcg_iters": s.pcg_iters, "pcg_residual": s.pcg_residual, "converged": bool(s.pcg_converged),
+                "nsub": s.nsub[0]}
+
+    def sky_mask(self, ground_height=None) -> np.ndarray:
+        gh = self.read_ground_height() if ground_height is None else np.asarray(ground_height)
+        y = np.arange(self.ny)[None, :, None]
+        return (y > gh.reshape(self.nz, self.nx)[:, None, :]).reshape(-1)
+
+    def read_ground_height(self):
+        return np.zeros(self.ng, np.int32) if getattr(self, "_gh", None) is None else self._gh
