@@ -184,6 +184,7 @@ def main():
     ap.add_argument("--semantics", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--shape", default=None, help="x,y,z (z vertical) override of the workload size")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -199,7 +200,8 @@ def main():
     from skewtcloudsim_gb300 import Environment, SolverConfig, sounding, build
     build.build()
 
-    init, dt, speed = sounding.workload(args.workload)
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
+    init, dt, speed = sounding.workload(args.workload, scale=shape)
     cfg = SolverConfig(semantics=args.semantics, precision=1 if args.mode == "mixed" else 0)
     env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
     env.init_from(init)

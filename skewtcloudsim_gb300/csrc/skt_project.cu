@@ -345,10 +345,9 @@ void launch_project(Env& e, float dtS) {
     for (int it = 0; it < e.cfg.pcg_max_iter; it += chunk) {
         const int n = std::min(chunk, e.cfg.pcg_max_iter - it);
         for (int k = 0; k < n; ++k) {
-            e.launches += 3;
-            { ProfScope ps(e, "pcg_matvec"); k_matvec<<<nblk, NT, 0, e.stream>>>(g, T, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
-            { ProfScope ps(e, "pcg_update"); k_update<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.s, e.As, e.pp, e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
-            { ProfScope ps(e, "pcg_search"); k_search<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.r, e.s, e.sc); }
+            { ProfScope ps(e, "pcg_matvec"); e.launches += 1; k_matvec<<<nblk, NT, 0, e.stream>>>(g, T, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
+            { ProfScope ps(e, "pcg_update"); e.launches += 1; k_update<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.s, e.As, e.pp, e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
+            { ProfScope ps(e, "pcg_search"); e.launches += 1; k_search<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.r, e.s, e.sc); }
         }
         cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
         cudaStreamSynchronize(e.stream);
