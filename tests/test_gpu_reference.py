@@ -4,9 +4,14 @@ The reference kernels are compiled unmodified from the reference sources into
 oracle/_ref/ref_<X>x<Y>x<Z>.cubin (oracle/build_ref.py) and driven by oracle/ref_harness.cpp.
 Each step starts all three implementations from the reference's state after the previous step,
 so every comparison is one step from identical inputs. Tolerance: relative L2 <= 1e-5 per sky
-field per step on the 16x32x16 grid, whose 16-wide ground tiles have no interior edges (the
-reference's advectGroundWaterGPU leaves interior tile halos uninitialised, so larger grids
-compare the sky fields that the ground stores do not feed within the step).
+field per step, and equal Courant substep counts.
+
+On grids wider than 16 cells in x or z the reference's advectGroundWaterGPU reads
+uninitialised shared memory at the interior edges of its 16x16 tiles
+(Game/kernelSky.cu:141-164 fills halos only at the domain edge); the garbage can reach the
+sky fields as non-finite values within a few steps. A step is compared only while the
+reference's own output is finite; the 16x32x16 grid has no interior tile edge and is compared
+on every step.
 """
 import json
 import os
@@ -60,7 +65,8 @@ def test_step_against_reference_kernels(gpu_lib, grid):
         env.update_gpu(dt, speed)
         gd = env.stats()
         m = ref.sky_mask()
-        row = {"step": step + 1, "ref_pcg": rd["pcg_iters"][0], "oracle_pcg": od["pcg_iters"], "gpu_pcg": gd["pcg_iters"],
+        finite = all(np.isfinite(ref.a[k][m]).all() for k in SKY)
+        row = {"ref_finite": bool(finite), "step": step + 1, "ref_pcg": rd["pcg_iters"][0], "oracle_pcg": od["pcg_iters"], "gpu_pcg": gd["pcg_iters"],
                "nsub_ref": rd["nsub"][0], "nsub_gpu": gd["nsub"]}
         for k in SKY:
             row[f"oracle_{k}"] = rel_l2(orc.a[k], ref.a[k], m)
@@ -68,8 +74,13 @@ def test_step_against_reference_kernels(gpu_lib, grid):
         report.append(row)
     _record(f"{X}x{Y}x{Z}", report)
     env.close()
+    if (X, Y, Z) == (16, 32, 16):
+        assert all(r["ref_finite"] for r in report)
+    assert report[0]["ref_finite"] or max(X, Z) > 16
     for row in report:
+        if not row["ref_finite"]:
+            break  # the reference's uninitialised ground-tile halos; later steps start from NaN
         assert row["nsub_ref"] == row["nsub_gpu"], row
-        if (X, Y, Z) == (16, 32, 16):
-            bad = {k: v for k, v in row.items() if (k.startswith("oracle_") or k.startswith("gpu_")) and v > 1e-5}
-            assert not bad, (row["step"], bad)
+        bad = {k: v for k, v in row.items() if (k.startswith("oracle_") or k.startswith("gpu_"))
+               and not k.endswith("_pcg") and v > 1e-5}
+        assert not bad, (row["step"], bad)
