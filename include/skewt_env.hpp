@@ -1,0 +1,86 @@
+// skewt_env.hpp — C++ adapter with the shape of the reference's environmentGPU class
+// (Game/environment.cuh:9-183), over the C ABI in skewt.h. Header-only; link libskewt_gb300.so.
+//
+// The reference's call sites map one to one:
+//   Game.EnvGPU().init(potTemp, velField, Qv, groundTemp, groundPressure, pressures, pressuresSmall)
+//       (Game/readTable.cpp:470)                        -> env.init(...)
+//   Game.EnvGPU().updateGPU(dt, speed)  (Game/game.cpp:56) -> env.updateGPU(dt, speed)
+//   getParamArray(parameter, direction) (Game/environment.cu:1076) -> env.getParamArray(...)
+//   editor::GPUSetEnv per-step readback (Game/editor.cpp:226)       -> env.readField(...)
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "skewt.h"
+
+namespace skewt {
+
+class Error : public std::runtime_error {
+public:
+    Error(skt_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+    skt_status status;
+};
+
+class EnvironmentGPU {
+public:
+    EnvironmentGPU(int nx, int ny_vertical, int nz, float voxel, const skt_solver_cfg* cfg = nullptr) {
+        skt_grid_desc g{nx, ny_vertical, nz, voxel};
+        check(skt_create(&g, cfg, &env_), nullptr);
+        n_ = size_t(nx) * ny_vertical * nz;
+    }
+    ~EnvironmentGPU() { skt_destroy(env_); }
+    EnvironmentGPU(const EnvironmentGPU&) = delete;
+    EnvironmentGPU& operator=(const EnvironmentGPU&) = delete;
+
+    // environmentGPU::init. velField is (u, v, w) per cell, like the reference's glm::vec3 array.
+    void init(const float* potTemps, const float* velField, const float* Qv, const float* groundTemp, const float* groundPres,
+              const float* pressures, const float* smallPressure, const int32_t* groundHeight, bool noise = true,
+              uint32_t seed = 100) {
+        check(skt_init(env_, potTemps, velField, Qv, groundTemp, groundPres, pressures, smallPressure, groundHeight,
+                       noise ? SKT_INIT_NOISE : 0u, seed));
+    }
+
+    // environmentGPU::updateGPU. Returns false when the pressure solve hit its iteration cap
+    // (the step is still done, as in the reference).
+    bool updateGPU(float dt, float speed, int nsteps = 1) {
+        const skt_status s = skt_step(env_, dt, speed, nsteps);
+        if (s == SKT_NOT_CONVERGED) return false;
+        check(s);
+        return true;
+    }
+
+    // environmentGPU::getParamArray
+    float* getParamArray(skt_param type, skt_direction windDir = SKT_RIGHT) {
+        float* p = nullptr;
+        check(skt_field_device_ptr(env_, type, windDir, &p));
+        return p;
+    }
+
+    // one field of editor::GPUSetEnv's readback
+    std::vector<float> readField(skt_param type, skt_direction windDir = SKT_RIGHT) {
+        std::vector<float> out(n_);
+        check(skt_read_field(env_, type, windDir, out.data(), out.size()));
+        return out;
+    }
+
+    skt_step_stats stats() {
+        skt_step_stats s{};
+        check(skt_stats(env_, &s));
+        return s;
+    }
+
+    skt_env* handle() { return env_; }
+
+private:
+    void check(skt_status s, const skt_env* e = reinterpret_cast<const skt_env*>(1)) {
+        if (s == SKT_OK) return;
+        throw Error(s, skt_last_error(e == reinterpret_cast<const skt_env*>(1) ? env_ : e));
+    }
+    skt_env* env_ = nullptr;
+    size_t n_ = 0;
+};
+
+}  // namespace skewt

@@ -74,3 +74,22 @@ def test_library_exports_every_declared_symbol():
     assert set(_lib.SIGNATURES) == names
     L = _lib.load(path)
     assert L.skt_version().startswith(b"skewt-gb300")
+
+
+def test_cpp_adapter_compiles_and_links(tmp_path):
+    """include/skewt_env.hpp (the environmentGPU-shaped C++ adapter) compiles against skewt.h and
+    links libskewt_gb300.so; the program only queries the version (no GPU work)."""
+    import subprocess
+    from skewtcloudsim_gb300 import build
+    lib = build.build()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "use_env.cpp"
+    src.write_text('#include "skewt_env.hpp"\n#include <cstdio>\n'
+                   'int main() { std::printf("%s\\n", skt_version()); skt_solver_cfg c; skt_default_config(&c);'
+                   ' return c.pcg_max_iter == 200 ? 0 : 1; }\n')
+    exe = tmp_path / "use_env"
+    libdir = os.path.dirname(lib)
+    subprocess.run(["g++", "-std=c++17", str(src), "-I", os.path.join(root, "include"), "-L", libdir, "-lskewt_gb300",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.startswith("skewt-gb300")
