@@ -158,7 +158,26 @@ skt_status skt_run_stage(skt_env* env, int stage, int arg, float dt, float speed
 skt_status skt_profile_enable(skt_env* env, int on);
 skt_status skt_profile_read(skt_env* env, char* buf, size_t n);
 
-/* Text of the last error on env (or of the last skt_create failure when env is NULL). */
+/* Allocation-free diffusion (no counterpart in the reference). For callers that cannot
+ * allocate device memory: a host framework that owns the device memory pool and forbids other
+ * allocations, or a running loop where a cudaMalloc would stall the device. It runs the
+ * diffusion stage (diffuseGPU's sweeps and boundary table, field_type 0..5 as there) on
+ * caller-owned device buffers: in_dev is read, out_dev receives the result (ground cells copied
+ * from in_dev). The one intermediate buffer lives in a static device array of
+ * SKT_NOALLOC_MAX_CELLS floats (8 MiB) that every GPU loading the library holds until exit;
+ * larger grids are rejected with SKT_INVALID_ARG (message in skt_last_error(NULL)). The first
+ * call on each device looks up that array's address, so make it before any stream capture.
+ * Calls share the array: calls whose work overlaps on the GPU race. Work is queued on `stream`
+ * (a cudaStream_t; NULL = default stream); the call does not synchronise. Nothing in the array
+ * needs clearing between calls (every value is written before it is read). */
+#define SKT_NOALLOC_MAX_CELLS (1u << 21)
+skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, int field_type, float dt_speed, int sweeps,
+                               const float* in_dev, float* out_dev, const int32_t* ground_height_dev,
+                               const float* default_column_dev, const float* p_dev, const float* ground_T_dev,
+                               const float* ground_p_dev, void* stream);
+
+/* Text of the last error on env (or, when env is NULL, of the last skt_create or
+ * skt_diffuse_noalloc failure on this thread). */
 const char* skt_last_error(const skt_env* env);
 
 /* Library version string. */

@@ -53,6 +53,10 @@ SIGNATURES = {
                                      ctypes.POINTER(StepStats)]),
     "skt_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "skt_profile_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "skt_diffuse_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                           ctypes.c_float, ctypes.c_int, c_float_p, c_float_p,
+                                           ctypes.POINTER(ctypes.c_int32), c_float_p, c_float_p, c_float_p, c_float_p,
+                                           ctypes.c_void_p]),
     "skt_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "skt_version": (ctypes.c_char_p, []),
 }

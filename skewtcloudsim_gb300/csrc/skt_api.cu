@@ -141,6 +141,10 @@ skt_status run_step(Env& e, float dt, float speed) {
 
 }  // namespace
 
+namespace skt {
+void set_global_error(const char* msg) { g_create_err = msg ? msg : ""; }
+}  // namespace skt
+
 extern "C" {
 
 void skt_default_config(skt_solver_cfg* c) {

@@ -1,6 +1,7 @@
 // Stencil kernels of the atmosphere step: diffusion, PPM advection, Courant max, sedimentation,
 // buoyancy and the equation of state.
 #include "skt_internal.cuh"
+#include "../../include/skewt.h"
 
 namespace skt {
 
@@ -434,6 +435,111 @@ void launch_new_pressure(Env& e) {
     ProfScope ps(e, "eos");
     e.launches += 1;
     k_new_pressure<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.p, e.rho, e.th, e.qv, e.Pg);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free diffusion of one caller-owned field.
+//
+// For callers that must not allocate device memory themselves: code running inside a host
+// framework that owns a fixed device memory pool and forbids outside allocations, or code on a
+// path where a cudaMalloc would synchronise the device or fail (for instance while a real-time
+// loop is running). Such callers pass their own input and output buffers; the one intermediate
+// buffer the sweeps need lives in the file-scope array below, reserved when the library loads
+// and held on every GPU that loads it until the process exits.
+// ---------------------------------------------------------------------------------------------
+
+namespace {
+
+constexpr unsigned kNoAllocMaxCells = 1u << 21;  // 2,097,152 cells: 8 MiB of scratch
+
+// Shared by every call on a device: it keeps the last call's contents. Nothing in it needs to
+// start at zero, because each sweep writes every sky cell before the next sweep reads it and
+// ground cells are never read. Calls whose work overlaps on the GPU race on it.
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocMaxCells];
+
+constexpr int kNoAllocMaxDevices = 64;
+float* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+__global__ void k_copy_all(const float* __restrict__ src, float* __restrict__ dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+}  // namespace
+
+void set_global_error(const char* msg);  // skt_last_error(NULL) text, defined in skt_api.cu
+
+extern "C" skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, int field_type, float dt_speed, int sweeps,
+                                          const float* in_dev, float* out_dev, const int32_t* ground_height_dev,
+                                          const float* default_column_dev, const float* p_dev, const float* ground_T_dev,
+                                          const float* ground_p_dev, void* stream) {
+    const long long n = (long long)nx * ny * nz;
+    if (nx < 1 || ny < 2 || nz < 1 || !(voxel > 0.0f) || sweeps < 0 || field_type < 0 || field_type > 5) {
+        set_global_error("skt_diffuse_noalloc: invalid grid, sweep count or field type");
+        return SKT_INVALID_ARG;
+    }
+    if (n > (long long)kNoAllocMaxCells) {
+        set_global_error("skt_diffuse_noalloc: nx*ny*nz exceeds SKT_NOALLOC_MAX_CELLS (2097152 cells); "
+                         "diffuse larger grids through skt_create/skt_step");
+        return SKT_INVALID_ARG;
+    }
+    if (!in_dev || !out_dev || !ground_height_dev || in_dev == out_dev) {
+        set_global_error("skt_diffuse_noalloc: null or aliased input/output buffer");
+        return SKT_INVALID_ARG;
+    }
+    if ((field_type == 0 && (!default_column_dev || !p_dev || !ground_T_dev || !ground_p_dev)) ||
+        ((field_type == 1 || field_type == 2 || field_type == 4) && !default_column_dev)) {
+        set_global_error("skt_diffuse_noalloc: this field type needs its default column (and, for theta, p/ground T/ground p)");
+        return SKT_INVALID_ARG;
+    }
+    // Set-up, once per device and with that device current: the address of the array. In host
+    // code its name only stands in for the device symbol, so the kernels get this pointer.
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_global_error("skt_diffuse_noalloc: no usable current CUDA device");
+        return SKT_CUDA_ERROR;
+    }
+    float* scratch = g_noalloc_ptr[dev];
+    if (!scratch) {
+        const cudaError_t err = cudaGetSymbolAddress((void**)&scratch, g_noalloc_scratch);
+        if (err != cudaSuccess || !scratch) {
+            set_global_error(cudaGetErrorString(err));
+            return SKT_CUDA_ERROR;
+        }
+        g_noalloc_ptr[dev] = scratch;
+    }
+    Grid g;
+    g.X = nx; g.Y = ny; g.Z = nz; g.XY = nx * ny; g.N = int(n); g.gh = ground_height_dev; g.vox = voxel;
+    int sides = NEUMANN, ground = DIRICHLET;
+    const float* def = default_column_dev;
+    switch (field_type) {  // diffuseGPU's boundary table, Game/environment.cu:603-638
+        case 0: sides = CUSTOM; ground = CUSTOM; break;
+        case 1: sides = CUSTOM; ground = DIRICHLET; break;
+        case 2: sides = CUSTOM; break;
+        case 3: def = nullptr; break;
+        case 4: sides = CUSTOM; break;
+        default: break;  // NEUMANN sides, DIRICHLET ground, custom column unused
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const float k = 0.005f * dt_speed / (voxel * voxel);
+    // out takes the input first so its ground cells keep their values; the sweeps then alternate
+    // between out and the scratch array so that the last one lands in out.
+    k_copy_all<<<(int(n) + 255) / 256, 256, 0, st>>>(in_dev, out_dev, int(n));
+    const float* src = in_dev;
+    for (int s = 0; s < sweeps; ++s) {
+        float* dst = ((sweeps - 1 - s) % 2 == 0) ? out_dev : scratch;
+        if (field_type == 0)
+            k_diffuse<true><<<cell_grid(g), dim3(BX, BY), 0, st>>>(g, src, dst, sides, ground, def, k, p_dev, ground_T_dev, ground_p_dev);
+        else
+            k_diffuse<false><<<cell_grid(g), dim3(BX, BY), 0, st>>>(g, src, dst, sides, ground, def, k, p_dev, ground_T_dev, ground_p_dev);
+        src = dst;
+    }
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_global_error(cudaGetErrorString(err));
+        return SKT_CUDA_ERROR;
+    }
+    return SKT_OK;
 }
 
 }  // namespace skt
