@@ -290,6 +290,232 @@ __global__ void __launch_bounds__(NT) k_search(Grid g, Tiles T, const float* __r
     }
 }
 
+// ---- vectorised PCG iteration (X % 4 == 0): float4 streams, FP32-compensated per-thread sums,
+// FP64 across threads and blocks --------------------------------------------------------------
+
+struct Kahan {  // compensated FP32 running sum
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+template <int NTH>
+__device__ __forceinline__ double block_sum_n(double v, double* sm, int tid) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((tid & 31) == 0) sm[tid >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (tid < 32) {
+        t = tid < (NTH / 32) ? sm[tid] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+template <int NTH>
+__device__ __forceinline__ float block_max_n(float v, float* sm, int tid) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((tid & 31) == 0) sm[tid >> 5] = v;
+    __syncthreads();
+    float t = 0.0f;
+    if (tid < 32) {
+        t = tid < (NTH / 32) ? sm[tid] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(0xffffffffu, t, o));
+    }
+    return t;
+}
+// publish() for any grid shape: bid = linear block id, nb = number of blocks
+__device__ __forceinline__ bool publish_n(Scalars* sc, double* partials, int bid, int nb, int tid, double sum, float mx, double& tot,
+                                          float& mxall) {
+    __shared__ bool last;
+    if (tid == 0) {
+        partials[bid] = sum;
+        partials[kMaxPartials + bid] = double(mx);
+        __threadfence();
+        const unsigned t = atomicAdd(&sc->done_blocks, 1u);
+        last = (t == unsigned(nb) - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    if (tid == 0) {
+        __threadfence();
+        double s = 0.0, m = 0.0;
+        for (int b = 0; b < nb; ++b) {
+            s += ((volatile double*)partials)[b];
+            const double mb = ((volatile double*)partials)[kMaxPartials + b];
+            m = mb > m ? mb : m;
+        }
+        tot = s;
+        mxall = float(m);
+        sc->done_blocks = 0;
+    }
+    return tid == 0;
+}
+
+constexpr int UT = 256;
+
+// p += alpha s, r -= alpha As, z = r/diag, z.r and the max residual, over all cells as float4
+// (ground cells hold s = As = r = 0 and diag 0, so they contribute nothing and stay zero).
+__global__ void __launch_bounds__(UT) k_update4(int n4, int xy4, const float4* __restrict__ aw, const float4* __restrict__ s,
+                                                const float4* __restrict__ As, float4* __restrict__ pp, float4* __restrict__ r,
+                                                int reference, float tol, int max_iter, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ double smd[UT / 32];
+    __shared__ float smf[UT / 32];
+    const float alpha = sc->alpha;
+    Kahan acc;
+    float mx = 0.0f;
+    for (int i = blockIdx.x * UT + threadIdx.x; i < n4; i += gridDim.x * UT) {
+        const float4 a = aw[i], sv = s[i], av = As[i];
+        float4 pv = pp[i], rv = r[i];
+        pv.x += alpha * sv.x; pv.y += alpha * sv.y; pv.z += alpha * sv.z; pv.w += alpha * sv.w;
+        rv.x = rv.x - alpha * av.x; rv.y = rv.y - alpha * av.y; rv.z = rv.z - alpha * av.z; rv.w = rv.w - alpha * av.w;
+        pp[i] = pv;
+        r[i] = rv;
+        const float z0 = rv.x * precon_of(a.x), z1 = rv.y * precon_of(a.y), z2 = rv.z * precon_of(a.z), z3 = rv.w * precon_of(a.w);
+        acc.add(z0 * rv.x);
+        acc.add(z1 * rv.y);
+        acc.add(z2 * rv.z);
+        acc.add(z3 * rv.w);
+        const bool absv = !reference || i < xy4;  // the reference takes |r| on the z = 0 plane only (Q4)
+        const float m0 = absv ? fabsf(rv.x) : rv.x, m1 = absv ? fabsf(rv.y) : rv.y;
+        const float m2 = absv ? fabsf(rv.z) : rv.z, m3 = absv ? fabsf(rv.w) : rv.w;
+        if (m0 > mx) mx = m0;
+        if (m1 > mx) mx = m1;
+        if (m2 > mx) mx = m2;
+        if (m3 > mx) mx = m3;
+    }
+    const double bs = block_sum_n<UT>(double(acc.s) - double(acc.c), smd, threadIdx.x);
+    const float bm = block_max_n<UT>(mx, smf, threadIdx.x);
+    double tot;
+    float mall;
+    if (publish_n(sc, partials, blockIdx.x, gridDim.x, threadIdx.x, bs, bm, tot, mall)) {
+        sc->iters += 1;
+        sc->residual = mall;
+        if (mall <= tol) {
+            sc->converged = 1;
+        } else if (sc->iters >= max_iter) {
+            sc->converged = 2;
+        } else {
+            sc->sigma1 = tot;
+            sc->beta_f = float(tot / sc->sigma0);
+            sc->sigma0 = tot;
+        }
+    }
+}
+
+// s = r/diag + beta s over all cells as float4
+__global__ void __launch_bounds__(UT) k_search4(int n4, const float4* __restrict__ aw, const float4* __restrict__ r, float4* __restrict__ s,
+                                                const Scalars* sc) {
+    if (sc->converged) return;
+    const float beta = sc->beta_f;
+    for (int i = blockIdx.x * UT + threadIdx.x; i < n4; i += gridDim.x * UT) {
+        const float4 a = aw[i], rv = r[i];
+        float4 sv = s[i];
+        sv.x = rv.x * precon_of(a.x) + beta * sv.x;
+        sv.y = rv.y * precon_of(a.y) + beta * sv.y;
+        sv.z = rv.z * precon_of(a.z) + beta * sv.z;
+        sv.w = rv.w * precon_of(a.w) + beta * sv.w;
+        s[i] = sv;
+    }
+}
+
+constexpr int MVY = 4;            // y rows per block
+constexpr int MVT = 32 * MVY;     // threads per block
+
+__device__ __forceinline__ float4 ld4(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
+__device__ __forceinline__ float4 f4zero() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+
+// As = A s and s.As with 4 cells per thread along x and a march along z that keeps the planes
+// z-1, z, z+1 of s and the previous plane's z-coefficient in registers. Neighbours outside the
+// domain read as 0; ground neighbours need no test because their s and coefficients are 0.
+__global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
+                                                 const float* __restrict__ az, const float* __restrict__ aw, const float* __restrict__ s,
+                                                 float* __restrict__ As, int reference, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ double smd[MVT / 32];
+    const int lane = threadIdx.x, tid = threadIdx.x + 32 * threadIdx.y;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * MVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const int X = g.X, XY = g.XY;
+    const int row = x0 + y * X;
+    Kahan acc;
+    float4 sb = f4zero(), scur = f4zero(), azb = f4zero();
+    if (act) {
+        const int c = row + zs * XY;
+        scur = ld4(s, c);
+        if (zs > 0) { sb = ld4(s, c - XY); azb = ld4(az, c - XY); }
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 sf = f4zero(), sd = f4zero(), su = f4zero(), ayd = f4zero(), cx = f4zero(), cy = f4zero(), cz = f4zero(), cw = f4zero();
+        int4 gh4 = make_int4(0, 0, 0, 0);
+        if (act) {
+            if (z + 1 < g.Z) sf = ld4(s, c + XY);
+            if (y > 0) { sd = ld4(s, c - X); ayd = ld4(ay, c - X); }
+            if (y + 1 < g.Y) su = ld4(s, c + X);
+            cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c);
+            gh4 = *reinterpret_cast<const int4*>(g.gh + x0 + z * X);
+        }
+        // x neighbours through the neighbouring lanes; the warp's edge lanes load them
+        float sl = __shfl_up_sync(0xffffffffu, scur.w, 1);
+        float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
+        float sr = __shfl_down_sync(0xffffffffu, scur.x, 1);
+        if (act && lane == 0) {
+            if (x0 > 0) { sl = s[c - 1]; axl = ax[c - 1]; } else { sl = 0.0f; axl = 0.0f; }
+        }
+        if (act && (lane == 31 || x0 + 4 >= X)) sr = (x0 + 4 < X) ? s[c + 4] : 0.0f;
+        if (act) {
+            float AL0 = axl, AL1 = cx.x, AL2 = cx.y, AL3 = cx.z;
+            float AD0 = ayd.x, AD1 = ayd.y, AD2 = ayd.z, AD3 = ayd.w;
+            float AB0 = azb.x, AB1 = azb.y, AB2 = azb.z, AB3 = azb.w;
+            if (reference) {
+                AL0 = char_trunc(AL0); AL1 = char_trunc(AL1); AL2 = char_trunc(AL2); AL3 = char_trunc(AL3);
+                AD0 = char_trunc(AD0); AD1 = char_trunc(AD1); AD2 = char_trunc(AD2); AD3 = char_trunc(AD3);
+                AB0 = char_trunc(AB0); AB1 = char_trunc(AB1); AB2 = char_trunc(AB2); AB3 = char_trunc(AB3);
+            }
+            float4 o;
+            o.x = cw.x * scur.x + ((AL0 * sl + AD0 * sd.x + AB0 * sb.x + cx.x * scur.y + cy.x * su.x + cz.x * sf.x));
+            o.y = cw.y * scur.y + ((AL1 * scur.x + AD1 * sd.y + AB1 * sb.y + cx.y * scur.z + cy.y * su.y + cz.y * sf.y));
+            o.z = cw.z * scur.z + ((AL2 * scur.y + AD2 * sd.z + AB2 * sb.z + cx.z * scur.w + cy.z * su.z + cz.z * sf.z));
+            o.w = cw.w * scur.w + ((AL3 * scur.z + AD3 * sd.w + AB3 * sb.w + cx.w * sr + cy.w * su.w + cz.w * sf.w));
+            if (y <= gh4.x) o.x = 0.0f;
+            if (y <= gh4.y) o.y = 0.0f;
+            if (y <= gh4.z) o.z = 0.0f;
+            if (y <= gh4.w) o.w = 0.0f;
+            *reinterpret_cast<float4*>(As + c) = o;
+            acc.add(o.x * scur.x);
+            acc.add(o.y * scur.y);
+            acc.add(o.z * scur.z);
+            acc.add(o.w * scur.w);
+        }
+        sb = scur;
+        scur = sf;
+        azb = cz;
+    }
+    const double bs = block_sum_n<MVT>(double(acc.s) - double(acc.c), smd, tid);
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    double tot;
+    float mall;
+    if (publish_n(sc, partials, bid, nb, tid, bs, 0.0f, tot, mall)) {
+        const double s1 = reference ? sc->sigma1 + tot : tot;
+        sc->sigma1 = s1;
+        sc->alpha = float(sc->sigma0 / s1);
+    }
+}
+
 // updatePressure (:1016-1030) followed by initDensity (:1432-1452)
 __global__ void __launch_bounds__(256) k_press_dens(Grid g, float* __restrict__ p, const float* __restrict__ pp, float* __restrict__ rho,
                                                     const float* __restrict__ th, const float* __restrict__ qv, const float* __restrict__ Pg) {
@@ -342,12 +568,33 @@ void launch_project(Env& e, float dtS) {
                                       e.sc, e.partials);
     }
     const int chunk = 8;
+    const bool vec = (g.X % 4) == 0;
+    // vectorised launch shapes: streams at 8 blocks/SM, the matvec's z chunks sized to fill the GPU
+    const int n4 = g.N / 4;
+    const int nstream = std::min(std::min((n4 + UT - 1) / UT, e.num_sms * 8), kMaxPartials);
+    const dim3 mvb(32, MVY);
+    const int gx = (g.X / 4 + 31) / 32, gy = (g.Y + MVY - 1) / MVY;
+    int zc = std::max(1, std::min(g.Z, (e.num_sms * 8 + gx * gy - 1) / (gx * gy)));
+    while (gx * gy * zc > kMaxPartials && zc > 1) --zc;
+    const int zlen = (g.Z + zc - 1) / zc;
+    zc = (g.Z + zlen - 1) / zlen;
+    const dim3 mvg(gx, gy, zc);
     for (int it = 0; it < e.cfg.pcg_max_iter; it += chunk) {
         const int n = std::min(chunk, e.cfg.pcg_max_iter - it);
         for (int k = 0; k < n; ++k) {
-            { ProfScope ps(e, "pcg_matvec"); e.launches += 1; k_matvec<<<nblk, NT, 0, e.stream>>>(g, T, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
-            { ProfScope ps(e, "pcg_update"); e.launches += 1; k_update<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.s, e.As, e.pp, e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
-            { ProfScope ps(e, "pcg_search"); e.launches += 1; k_search<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.r, e.s, e.sc); }
+            if (vec) {
+                { ProfScope ps(e, "pcg_matvec"); e.launches += 1;
+                  k_matvec4<<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
+                { ProfScope ps(e, "pcg_update"); e.launches += 1;
+                  k_update4<<<nstream, UT, 0, e.stream>>>(n4, g.XY / 4, (const float4*)e.aw, (const float4*)e.s, (const float4*)e.As,
+                                                          (float4*)e.pp, (float4*)e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
+                { ProfScope ps(e, "pcg_search"); e.launches += 1;
+                  k_search4<<<nstream, UT, 0, e.stream>>>(n4, (const float4*)e.aw, (const float4*)e.r, (float4*)e.s, e.sc); }
+            } else {
+                { ProfScope ps(e, "pcg_matvec"); e.launches += 1; k_matvec<<<nblk, NT, 0, e.stream>>>(g, T, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
+                { ProfScope ps(e, "pcg_update"); e.launches += 1; k_update<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.s, e.As, e.pp, e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
+                { ProfScope ps(e, "pcg_search"); e.launches += 1; k_search<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.r, e.s, e.sc); }
+            }
         }
         cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
         cudaStreamSynchronize(e.stream);

@@ -2,6 +2,7 @@
 // buoyancy and the equation of state.
 #include "skt_internal.cuh"
 #include "../../include/skewt.h"
+#include <algorithm>
 
 namespace skt {
 
@@ -57,6 +58,71 @@ __global__ void __launch_bounds__(256) k_diffuse(Grid g, const float* __restrict
         }
     }
     out[c] = (in[c] + k * (l + r + u + d + f + b)) / (1 + 6 * k);
+}
+
+// Vectorised sweep for flat terrain (ground = the y = 0 layer) and X % 4 == 0: four cells per
+// thread along x, a march along z holding the planes z-1, z, z+1 in registers, x neighbours from
+// the neighbouring lanes. Same arithmetic and ghost values as k_diffuse.
+constexpr int DVY = 4;
+__device__ __forceinline__ float4 ld4f(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
+__device__ __forceinline__ float side_val(int bc, float own, float d) { return bc == NEUMANN ? own : (bc == DIRICHLET ? 0.0f : d); }
+
+template <bool THETA>
+__global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out, int sides,
+                                                       int ground, const float* __restrict__ def, float k, const float* __restrict__ p,
+                                                       const float* __restrict__ Tg, const float* __restrict__ Pg) {
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * DVY + threadIdx.y + 1;  // sky rows start at y = 1
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const int X = g.X, XY = g.XY;
+    const int row = x0 + y * X;
+    const float dy = act ? (def ? def[y] : 0.0f) : 0.0f;
+    const float dy0 = def ? def[0] : 0.0f;
+    const float inv = 1 + 6 * k;
+    float4 qb = make_float4(0, 0, 0, 0), qc = qb;
+    if (act) {
+        qc = ld4f(in, row + zs * XY);
+        if (zs > 0) qb = ld4f(in, row + (zs - 1) * XY);
+        else qb = make_float4(side_val(sides, qc.x, dy), side_val(sides, qc.y, dy), side_val(sides, qc.z, dy), side_val(sides, qc.w, dy));
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 qf = qb, qd = qb, qu = qb;
+        if (act) {
+            if (z + 1 < g.Z) qf = ld4f(in, c + XY);
+            else qf = make_float4(side_val(sides, qc.x, dy), side_val(sides, qc.y, dy), side_val(sides, qc.z, dy), side_val(sides, qc.w, dy));
+            if (y > 1) qd = ld4f(in, c - X);
+            else {
+                const float gv = ground == DIRICHLET ? 0.0f : dy0;
+                qd = make_float4(gv, gv, gv, gv);
+            }
+            if (y + 1 < g.Y) qu = ld4f(in, c + X);
+            else qu = make_float4(side_val(sides, qc.x, dy), side_val(sides, qc.y, dy), side_val(sides, qc.z, dy), side_val(sides, qc.w, dy));
+        }
+        float ql = __shfl_up_sync(0xffffffffu, qc.w, 1);
+        float qr = __shfl_down_sync(0xffffffffu, qc.x, 1);
+        if (act) {
+            if (lane == 0) ql = x0 > 0 ? in[c - 1] : side_val(sides, qc.x, dy);
+            if (lane == 31 || x0 + 4 >= X) qr = (x0 + 4 < X) ? in[c + 4] : side_val(sides, qc.w, dy);
+            if (THETA && y == 1) {  // theta's ground face (diffuseRedBlack :97)
+                const int gi = x0 + z * X;
+                qd.x = theta_ground(p, Tg, Pg, c, gi);
+                qd.y = theta_ground(p, Tg, Pg, c + 1, gi + 1);
+                qd.z = theta_ground(p, Tg, Pg, c + 2, gi + 2);
+                qd.w = theta_ground(p, Tg, Pg, c + 3, gi + 3);
+            }
+            float4 o;
+            o.x = (qc.x + k * (ql + qc.y + qu.x + qd.x + qf.x + qb.x)) / inv;
+            o.y = (qc.y + k * (qc.x + qc.z + qu.y + qd.y + qf.y + qb.y)) / inv;
+            o.z = (qc.z + k * (qc.y + qc.w + qu.z + qd.z + qf.z + qb.z)) / inv;
+            o.w = (qc.w + k * (qc.z + qr + qu.w + qd.w + qf.w + qb.w)) / inv;
+            *reinterpret_cast<float4*>(out + c) = o;
+        }
+        qb = qc;
+        qc = qf;
+    }
 }
 
 // advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp)
@@ -147,6 +213,155 @@ __global__ void __launch_bounds__(256) k_ppm(Grid g, const float* __restrict__ i
     out[c] = nq / nr;
 }
 
+// One cell of a directional PPM pass from its 5-value windows (q and the density companion):
+// the same arithmetic as k_ppm.
+__device__ __forceinline__ float ppm_cell(const float* q, const float* o, float vc, float vm, float dt, float vox) {
+    float nq, nr;
+    {
+        float L, C, R;
+        if (vc >= 0.0f) { L = q[1]; C = q[2]; R = q[3]; } else { L = q[4]; C = q[3]; R = q[2]; }
+        const float fp = ppm_flux(vc, L, C, R, dt, vox);
+        if (vm < 0.0f) { L = q[3]; C = q[2]; R = q[1]; } else { L = q[0]; C = q[1]; R = q[2]; }
+        const float fm = ppm_flux(vm, L, C, R, dt, vox);
+        nq = q[2] - (dt / vox) * (fp - fm);
+    }
+    {
+        float L, C, R;
+        if (vc >= 0.0f) { L = o[1]; C = o[2]; R = o[3]; } else { L = o[4]; C = o[3]; R = o[2]; }
+        const float fp = ppm_flux(vc, L, C, R, dt, vox);
+        if (vm < 0.0f) { L = o[3]; C = o[2]; R = o[1]; } else { L = o[0]; C = o[1]; R = o[2]; }
+        const float fm = ppm_flux(vm, L, C, R, dt, vox);
+        nr = 1.0f - (dt / vox) * (fp - fm);
+    }
+    return nq / nr;
+}
+
+__device__ __forceinline__ float comp(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+
+// Vectorised PPM pass for flat terrain and X % 4 == 0 (four cells per thread along x; the Z pass
+// marches with a five-plane window in registers).
+template <int AXIS>
+__global__ void __launch_bounds__(32 * DVY) k_ppm4(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
+                                                   const float* __restrict__ vel, const float* __restrict__ def, int sides, int ground,
+                                                   const float* __restrict__ defU, const float* __restrict__ defW, float dtFull,
+                                                   int nsub_host, int half, const Scalars* __restrict__ sc, int slot) {
+    int nsub = nsub_host;
+    if (sc) {
+        nsub = sc->nsub;
+        if (slot >= nsub) return;
+    }
+    const float dtSub = dtFull / float(nsub);
+    const float dt = half ? dtSub * 0.5f : dtSub;
+    const float vox = g.vox;
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * DVY + threadIdx.y + 1;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const int X = g.X, XY = g.XY;
+    const int row = x0 + y * X;
+    const float dy = act ? (def ? def[y] : 0.0f) : 0.0f;
+    const float dyt = def ? def[g.Y - 1] : 0.0f;
+    const float dg0 = def ? def[0] : 0.0f;
+    const float gq = bc_val(ground, 0.0f, dg0);   // ground ghost of q (ground is never NEUMANN here)
+    const float go = bc_val(ground, 1.0f, 1.0f);  // ground ghost of the density companion
+    const float so = bc_val(sides, 1.0f, 1.0f);   // side ghost of the density companion
+    if (AXIS == 2) {
+        // window planes z-2 .. z+2
+        float4 w0 = make_float4(0, 0, 0, 0), w1 = w0, w2 = w0, w3 = w0, w4 = w0, vb = w0;
+        auto side4 = [&](const float4& b) {
+            return make_float4(bc_val(sides, b.x, dy), bc_val(sides, b.y, dy), bc_val(sides, b.z, dy), bc_val(sides, b.w, dy));
+        };
+        if (act) {
+            w2 = ld4f(in, row + zs * XY);
+            w1 = zs >= 1 ? ld4f(in, row + (zs - 1) * XY) : side4(w2);
+            w0 = zs >= 2 ? ld4f(in, row + (zs - 2) * XY) : (zs == 1 ? side4(w1) : side4(w2));
+            w3 = zs + 1 < g.Z ? ld4f(in, row + (zs + 1) * XY) : side4(w2);
+            if (zs > 0) vb = ld4f(vel, row + (zs - 1) * XY);
+        }
+        for (int z = zs; z < ze; ++z) {
+            const int c = row + z * XY;
+            if (act) {
+                if (z + 2 < g.Z) w4 = ld4f(in, c + 2 * XY);
+                else w4 = z + 1 < g.Z ? side4(w3) : side4(w2);
+                const float4 vc4 = ld4f(vel, c);
+                float4 vm4 = vb;
+                if (z == 0) {
+                    const float cu = defW[y];
+                    vm4 = make_float4(bc_val(sides, vc4.x, cu), bc_val(sides, vc4.y, cu), bc_val(sides, vc4.z, cu), bc_val(sides, vc4.w, cu));
+                }
+                float4 o4;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float q[5] = {comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k)};
+                    const float o[5] = {z >= 2 ? 1.0f : so, z >= 1 ? 1.0f : so, 1.0f, z + 1 < g.Z ? 1.0f : so, z + 2 < g.Z ? 1.0f : so};
+                    const float r = ppm_cell(q, o, comp(vc4, k), comp(vm4, k), dt, vox);
+                    if (k == 0) o4.x = r; else if (k == 1) o4.y = r; else if (k == 2) o4.z = r; else o4.w = r;
+                }
+                *reinterpret_cast<float4*>(out + c) = o4;
+                vb = vc4;
+            }
+            w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+        }
+        return;
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        if (AXIS == 0) {
+            float4 qc = make_float4(0, 0, 0, 0), uc = qc;
+            if (act) { qc = ld4f(in, c); uc = ld4f(vel, c); }
+            float qm2 = __shfl_up_sync(0xffffffffu, qc.z, 1), qm1 = __shfl_up_sync(0xffffffffu, qc.w, 1);
+            float qp4 = __shfl_down_sync(0xffffffffu, qc.x, 1), qp5 = __shfl_down_sync(0xffffffffu, qc.y, 1);
+            float um1 = __shfl_up_sync(0xffffffffu, uc.w, 1);
+            if (!act) continue;
+            if (lane == 0) {
+                if (x0 >= 2) { qm2 = in[c - 2]; qm1 = in[c - 1]; um1 = vel[c - 1]; }
+                else { qm2 = qm1 = bc_val(sides, qc.x, dy); um1 = bc_val(sides, uc.x, defU[y]); }
+            }
+            if (lane == 31 || x0 + 4 >= X) {
+                if (x0 + 4 < X) { qp4 = in[c + 4]; qp5 = in[c + 5]; }
+                else { qp4 = qp5 = bc_val(sides, qc.w, dy); }
+            }
+            const float w[8] = {qm2, qm1, qc.x, qc.y, qc.z, qc.w, qp4, qp5};
+            const float vcs[4] = {uc.x, uc.y, uc.z, uc.w};
+            const float vms[4] = {um1, uc.x, uc.y, uc.z};
+            float4 o4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int x = x0 + k;
+                const float o[5] = {x >= 2 ? 1.0f : so, x >= 1 ? 1.0f : so, 1.0f, x + 1 < X ? 1.0f : so, x + 2 < X ? 1.0f : so};
+                const float r = ppm_cell(&w[k], o, vcs[k], vms[k], dt, vox);
+                if (k == 0) o4.x = r; else if (k == 1) o4.y = r; else if (k == 2) o4.z = r; else o4.w = r;
+            }
+            *reinterpret_cast<float4*>(out + c) = o4;
+        } else {
+            if (!act) continue;
+            const float4 qc = ld4f(in, c), vc4 = ld4f(vel, c);
+            const float4 gq4 = make_float4(gq, gq, gq, gq);
+            const float4 qd1 = y >= 2 ? ld4f(in, c - X) : gq4;
+            const float4 qd2 = y >= 3 ? ld4f(in, c - 2 * X) : gq4;
+            float4 qu1, qu2;
+            if (y + 1 < g.Y) qu1 = ld4f(in, c + X);
+            else qu1 = make_float4(bc_val(sides, qc.x, dy), bc_val(sides, qc.y, dy), bc_val(sides, qc.z, dy), bc_val(sides, qc.w, dy));
+            if (y + 2 < g.Y) qu2 = ld4f(in, c + 2 * X);
+            else if (y + 1 < g.Y) {
+                const float4 b = qu1;  // the clamped cell is the top row y+1 = Y-1
+                qu2 = make_float4(bc_val(sides, b.x, dyt), bc_val(sides, b.y, dyt), bc_val(sides, b.z, dyt), bc_val(sides, b.w, dyt));
+            } else qu2 = qu1;
+            const float4 vm4 = y >= 2 ? ld4f(vel, c - X) : make_float4(0, 0, 0, 0);  // face below y = 1 is ground: 0
+            const float o2[5] = {y >= 3 ? 1.0f : go, y >= 2 ? 1.0f : go, 1.0f, y + 1 < g.Y ? 1.0f : so, y + 2 < g.Y ? 1.0f : so};
+            float4 o4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float q[5] = {comp(qd2, k), comp(qd1, k), comp(qc, k), comp(qu1, k), comp(qu2, k)};
+                const float r = ppm_cell(q, o2, comp(vc4, k), comp(vm4, k), dt, vox);
+                if (k == 0) o4.x = r; else if (k == 1) o4.y = r; else if (k == 2) o4.z = r; else o4.w = r;
+            }
+            *reinterpret_cast<float4*>(out + c) = o4;
+        }
+    }
+}
+
 // copy the sky cells of src into dst (the end-of-substep copy, Game/environment.cu:805)
 __global__ void __launch_bounds__(256) k_copy_sky(Grid g, const float* __restrict__ src, float* __restrict__ dst, const Scalars* __restrict__ sc, int slot) {
     if (sc && slot >= sc->nsub) return;
@@ -155,6 +370,16 @@ __global__ void __launch_bounds__(256) k_copy_sky(Grid g, const float* __restric
     if (is_ground(g, x, y, z)) return;
     const int c = cidx(g, x, y, z);
     dst[c] = src[c];
+}
+
+// flat terrain: copy rows y >= 1 of every plane as float4
+__global__ void __launch_bounds__(256) k_copy_sky4(int n4, int X4, int Y, const float4* __restrict__ src, float4* __restrict__ dst,
+                                                   const Scalars* __restrict__ sc, int slot) {
+    if (sc && slot >= sc->nsub) return;
+    for (int i = blockIdx.x * 256 + threadIdx.x; i < n4; i += gridDim.x * 256) {
+        if ((i / X4) % Y == 0) continue;  // the ground layer
+        dst[i] = src[i];
+    }
 }
 
 // Max over sky cells of three fields (getMaxDivergence Game/kernelSky.cu:910-953 applied to
@@ -342,16 +567,34 @@ void launch_diffuse(Env& e, float* f, int type, float dtS) {
     cudaMemcpyAsync(e.tB, f, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
     float* a = e.tA;
     float* o = e.tB;
+    const bool vec = e.flat && (g.X % 4) == 0;
+    const int gx = (g.X / 4 + 31) / 32, gy = (g.Y - 1 + DVY - 1) / DVY;
+    int zc = std::max(1, std::min(g.Z, (e.num_sms * 16 + gx * gy - 1) / (gx * gy)));
+    const int zlen = (g.Z + zc - 1) / zc;
+    zc = (g.Z + zlen - 1) / zlen;
     for (int s = 0; s < sweeps; ++s) {
         const float* in = (s % 2 == 0) ? a : o;
         float* out = (s % 2 == 0) ? o : a;
+        if (vec) {
+            if (type == 0)
+                k_diffuse4<true><<<dim3(gx, gy, zc), dim3(32, DVY), 0, e.stream>>>(g, zlen, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
+            else
+                k_diffuse4<false><<<dim3(gx, gy, zc), dim3(32, DVY), 0, e.stream>>>(g, zlen, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
+            continue;
+        }
         if (type == 0)
             k_diffuse<true><<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
         else
             k_diffuse<false><<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
     }
     const float* res = (sweeps % 2 == 0) ? a : o;
-    k_copy_sky<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, res, f, nullptr, 0);
+    if (vec) {
+        const int n4 = g.N / 4;
+        k_copy_sky4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)res, (float4*)f,
+                                                                                     nullptr, 0);
+    } else {
+        k_copy_sky<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, res, f, nullptr, 0);
+    }
 }
 
 // advectPPMWGPU Game/environment.cu:692-824. With host_sync the substep count is read back as
@@ -379,8 +622,40 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     const dim3 grd = cell_grid(g), blk(BX, BY);
     float* A = f;
     float* O = e.tA;
+    const bool vec = e.flat && (g.X % 4) == 0;
+    const int gx = (g.X / 4 + 31) / 32, gy = (g.Y - 1 + DVY - 1) / DVY;
+    int zc = std::max(1, std::min(g.Z, (e.num_sms * 16 + gx * gy - 1) / (gx * gy)));
+    const int zlen = (g.Z + zc - 1) / zc;
+    zc = (g.Z + zlen - 1) / zlen;
+    const dim3 vg(gx, gy, zc), vb(32, DVY);
+    // the Z pass marches: fewer, longer z chunks
+    int zc2 = std::max(1, std::min(g.Z, (e.num_sms * 8 + gx * gy - 1) / (gx * gy)));
+    const int zlen2 = (g.Z + zc2 - 1) / zc2;
+    zc2 = (g.Z + zlen2 - 1) / zlen2;
+    const dim3 vg2(gx, gy, zc2);
+    const int n4 = g.N / 4;
+    const int ncopy = std::min((n4 + 255) / 256, e.num_sms * 8);
     e.launches += 6LL * slots;
     for (int i = 0; i < slots; ++i) {
+        if (vec) {
+            k_ppm4<0><<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+            const float* vy = e.v;
+            if (f == e.v) {
+                cudaMemcpyAsync(e.tB, e.v, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
+                vy = e.tB;
+            }
+            k_ppm4<1><<<vg, vb, 0, e.stream>>>(g, zlen, O, A, vy, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+            k_ppm4<2><<<vg2, vb, 0, e.stream>>>(g, zlen2, A, O, e.w, def, sides, ground, e.defU, e.defW, dtS, nsub, 0, chk, i);
+            vy = e.v;
+            if (f == e.v) {
+                cudaMemcpyAsync(e.tB, e.v, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
+                vy = e.tB;
+            }
+            k_ppm4<1><<<vg, vb, 0, e.stream>>>(g, zlen, O, A, vy, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+            k_ppm4<0><<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+            k_copy_sky4<<<ncopy, 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)O, (float4*)A, chk, i);
+            continue;
+        }
         // pass 1: X half, A -> O (velocity u as it stands: for f == u this is A)
         k_ppm<0><<<grd, blk, 0, e.stream>>>(g, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
         // pass 2: Y half, O -> A; the velocity is v as it stands before the pass (for f == v: q0)

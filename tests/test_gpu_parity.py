@@ -181,3 +181,59 @@ def test_full_step_parity(gpu_lib, sem):
         # carry the oracle state forward so each step is compared from identical inputs
         push_oracle_to_env(st, env)
     env.close()
+
+
+@pytest.mark.parametrize("ftype", [0, 1, 2, 3, 4, 5])
+def test_diffusion_large_coefficient(gpu_lib, developed, ftype):
+    """k = 0.005*dt/vox^2 = 0.1 (dt = 2e5 s): at the workloads' k ~ 2.5e-7 a wrong stencil would
+    hide below the tolerance, so the stage is also compared where every term matters."""
+    init, dt, speed, st0 = developed
+    st = _clone(st0)
+    env = make_env(init)
+    push_oracle_to_env(st, env)
+    big = 2.0e5
+    env.run_stage(0, ftype, big)
+    st.stage(oracle_cfg(), 0, ftype, big)
+    name = ["th", "qv", "u", "v", "w", "qw"][ftype]
+    l2, mx = compare(env, st, names=(name,), ground=())[name]
+    assert mx <= STAGE_TOL, (name, l2, mx)
+    env.close()
+
+
+@pytest.mark.parametrize("shape", [(30, 18, 20), (36, 28, 24)])
+def test_full_step_parity_scalar_paths(gpu_lib, shape):
+    """Grids whose x size is not a multiple of 4 (30) use the scalar kernels, the others the
+    vectorised ones; both must match the oracle."""
+    init, dt, speed = small_case(shape)
+    st = oracle.OracleState(init, np.float32)
+    env = make_env(init)
+    for step in range(2):
+        od = st.step(oracle_cfg(), dt, speed)
+        env.update_gpu(dt, speed)
+        assert env.stats()["nsub"] == od["nsub"]
+        res = compare(env, st)
+        bad = {k: v for k, v in res.items() if v[0] > STEP_TOL}
+        assert not bad, (step, bad)
+        push_oracle_to_env(st, env)
+    env.close()
+
+
+def test_full_step_parity_terrain(gpu_lib):
+    """A non-flat heightfield (up to 3 ground cells) exercises the general ghost rule."""
+    from skewtcloudsim_gb300 import sounding
+    init, dt, speed = small_case((32, 32, 32))
+    X, Z = init.nx, init.nz
+    xx, zz = np.meshgrid(np.arange(X), np.arange(Z))
+    gh = np.clip(np.round(3.0 * np.exp(-((xx - 12) ** 2 + (zz - 18) ** 2) / 40.0)), 0, 3).astype(np.int32).reshape(-1)
+    init.ground_height = gh
+    st = oracle.OracleState(init, np.float32)
+    env = make_env(init)
+    for step in range(2):
+        od = st.step(oracle_cfg(), dt, speed)
+        env.update_gpu(dt, speed)
+        assert env.stats()["nsub"] == od["nsub"]
+        res = compare(env, st)
+        bad = {k: v for k, v in res.items() if v[0] > STEP_TOL}
+        assert not bad, (step, bad)
+        push_oracle_to_env(st, env)
+    env.close()
