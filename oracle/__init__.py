@@ -69,10 +69,12 @@ def lib():
             g = getattr(L, f"oc_init_{suf}")
             g.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_int]
             g.restype = ctypes.c_int
-        L.oc_stage_f32.argtypes = [ctypes.POINTER(OcConfig), ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                   ctypes.POINTER(OcState), ctypes.c_int, ctypes.c_int, ctypes.c_float,
-                                   ctypes.c_float, ctypes.POINTER(OcDiag)]
-        L.oc_stage_f32.restype = ctypes.c_int
+        for suf in ("f32", "f64"):
+            f = getattr(L, f"oc_stage_{suf}")
+            f.argtypes = [ctypes.POINTER(OcConfig), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                          ctypes.POINTER(OcState), ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                          ctypes.c_float, ctypes.POINTER(OcDiag)]
+            f.restype = ctypes.c_int
         L.oc_irradiance.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
         L.oc_irradiance.restype = ctypes.c_float
         L.oc_num_threads.restype = ctypes.c_int
@@ -147,11 +149,11 @@ class OracleState:
                 "converged": bool(d.converged)}
 
     def stage(self, cfg: Config, stage: int, arg: int = 0, dt: float = 0.5, speed: float = 1.0):
-        assert self.dtype == np.float32
         st = self._cstate()
         d = OcDiag()
         c = cfg.c(self.voxel)
-        rc = lib().oc_stage_f32(ctypes.byref(c), self.X, self.Y, self.Z, ctypes.byref(st), stage, arg, dt, speed,
+        fn = lib().oc_stage_f32 if self.dtype == np.float32 else lib().oc_stage_f64
+        rc = fn(ctypes.byref(c), self.X, self.Y, self.Z, ctypes.byref(st), stage, arg, dt, speed,
                                 ctypes.byref(d))
         if rc != 0:
             raise RuntimeError(f"oracle stage failed: {rc}")

@@ -1132,35 +1132,37 @@ int oc_num_threads(void) {
 #endif
 }
 
+}  // extern "C"
+
 // Single-stage entry points used by the per-kernel parity tests.
-int oc_stage_f32(const oc_config* c, int X, int Y, int Z, oc_state* st, int stage, int arg, float dt, float speed, oc_diag* d) {
-    State<float> s = unpack<float>(st);
+template <class T> static int stage_impl(const oc_config* c, int X, int Y, int Z, oc_state* st, int stage, int arg, float dt, float speed, oc_diag* d) {
+    State<T> s = unpack<T>(st);
     Grid g{X, Y, Z, s.gh};
     Config cf = cfg_of(c);
-    static const Micro<float> M;
-    static const Gammas<float> Gm;
-    std::vector<float> zero(Y, 0.f);
+    static const Micro<T> M;
+    static const Gammas<T> Gm;
+    std::vector<T> zero(Y, T(0));
     Diag dg{};
     switch (stage) {
-        case 0: diffuse(g, cf, s, arg == 0 ? s.th : arg == 1 ? s.qv : arg == 2 ? s.u : arg == 3 ? s.v : arg == 4 ? s.w : s.qw, arg, dt); break;
+        case 0: diffuse(g, cf, s, arg == 0 ? s.th : arg == 1 ? s.qv : arg == 2 ? s.u : arg == 3 ? s.v : arg == 4 ? s.w : s.qw, arg, T(dt)); break;
         case 1: {  // advect field arg (0 th,1 u,2 v,3 w,4 qv,5 qw)
-            float* f[6] = {s.th, s.u, s.v, s.w, s.qv, s.qw};
-            const float* df[6] = {s.isenT, s.defU, zero.data(), s.defW, s.isenQv, zero.data()};
+            T* f[6] = {s.th, s.u, s.v, s.w, s.qv, s.qw};
+            const T* df[6] = {s.isenT, s.defU, zero.data(), s.defW, s.isenQv, zero.data()};
             Bounds bb[6] = {{CUSTOM, CUSTOM}, {CUSTOM, DIRICHLET}, {DIRICHLET, DIRICHLET}, {CUSTOM, DIRICHLET}, {CUSTOM, CUSTOM}, {DIRICHLET, DIRICHLET}};
-            dg.nsub[0] = advect_field(g, cf, s, f[arg], df[arg], bb[arg], dt);
+            dg.nsub[0] = advect_field(g, cf, s, f[arg], df[arg], bb[arg], T(dt));
             break;
         }
-        case 2: buoyancy(g, s, dt); break;
-        case 3: init_density(g, s); project(g, cf, s, dt, dg); break;
-        case 4: microphysics_sky(g, s, dt, speed, M); break;
-        case 5: advect_precip(g, cf, s, arg == 0 ? s.qr : arg == 1 ? s.qs : s.qi, arg, dt, Gm); break;
+        case 2: buoyancy(g, s, T(dt)); break;
+        case 3: init_density(g, s); project(g, cf, s, T(dt), dg); break;
+        case 4: microphysics_sky(g, s, T(dt), T(speed), M); break;
+        case 5: advect_precip(g, cf, s, arg == 0 ? s.qr : arg == 1 ? s.qs : s.qi, arg, T(dt), Gm); break;
         case 6: {
-            const float irr = irradiance(float(s.sim_time), s.day, s.longitude, s.sun);
-            ground_stage(g, cf, s, dt, speed, irr, M);
-            set_temps_at_ground(g, s, dt * speed);  // the GPU fuses this into its ground stage
+            const T irr = T(irradiance(float(s.sim_time), s.day, s.longitude, s.sun));
+            ground_stage(g, cf, s, T(dt), T(speed), irr, M);
+            set_temps_at_ground(g, s, T(dt) * T(speed));  // the GPU fuses this into its ground stage
             break;
         }
-        case 7: set_temps_at_ground(g, s, dt * speed); break;
+        case 7: set_temps_at_ground(g, s, T(dt) * T(speed)); break;
         case 8: init_density(g, s); break;
         case 9: new_pressure(g, s); break;
         default: return -1;
@@ -1169,4 +1171,12 @@ int oc_stage_f32(const oc_config* c, int X, int Y, int Z, oc_state* st, int stag
     return 0;
 }
 
+
+extern "C" {
+int oc_stage_f32(const oc_config* c, int X, int Y, int Z, oc_state* st, int stage, int arg, float dt, float speed, oc_diag* d) {
+    return stage_impl<float>(c, X, Y, Z, st, stage, arg, dt, speed, d);
+}
+int oc_stage_f64(const oc_config* c, int X, int Y, int Z, oc_state* st, int stage, int arg, float dt, float speed, oc_diag* d) {
+    return stage_impl<double>(c, X, Y, Z, st, stage, arg, dt, speed, d);
+}
 }  // extern "C"

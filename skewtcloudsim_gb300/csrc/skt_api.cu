@@ -247,6 +247,14 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     e.gam.Qr = tgammaf(4.0f + b);
     e.gam.Qs = tgammaf(4.0f + d);
     e.gam.Qi = e.gam.Qs;
+    if (e.cfg.precision == 1) {
+        e.cfg.semantics = SKT_SEM_TEXTBOOK;  // CG needs the symmetric operator
+        if (!mg_allocate(e)) {
+            g_create_err = "mixed precision needs grid sizes that halve down to <= 4096 cells (even nx, ny, nz at every level)";
+            skt_destroy(h);
+            return SKT_INVALID_ARG;
+        }
+    }
     const skt_status st = cuda_check(e, "create");
     if (st != SKT_OK) {
         g_create_err = e.err;
@@ -266,6 +274,7 @@ void skt_destroy(skt_env* env) {
     if (e.ev0) cudaEventDestroy(e.ev0);
     if (e.ev1) cudaEventDestroy(e.ev1);
     if (e.pool) cudaFree(e.pool);
+    if (e.mg_pool) cudaFree(e.mg_pool);
     if (e.host_sc) cudaFreeHost(e.host_sc);
     if (e.stream) cudaStreamDestroy(e.stream);
     delete env;

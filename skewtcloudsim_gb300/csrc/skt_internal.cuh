@@ -78,8 +78,17 @@ struct Scalars {
     double rnorm0;                    // mixed mode: initial residual norm
     double rnorm;                     // mixed mode: current residual norm
     int outer;                        // mixed mode: refinement steps
-    int pad;
+    float inner_tol;                  // mixed mode: max residual at the start of the inner solve
+    int outer_inner_total;            // mixed mode: inner iterations summed over the refinement
+    int refine_done;                  // mixed mode: relative FP64 residual met refine_tol
 };
+
+// one coarse level of the multigrid preconditioner (A-form coefficients and work vectors)
+struct MgLevel {
+    int X = 0, Y = 0, Z = 0;
+    float *ax = nullptr, *ay = nullptr, *az = nullptr, *aw = nullptr, *x = nullptr, *x2 = nullptr, *b = nullptr;
+};
+constexpr int kMaxMgLevels = 12;
 
 constexpr int kMaxPartials = 4096;
 
@@ -141,6 +150,10 @@ struct Env {
     // graph
     cudaGraphExec_t graph_exec = nullptr;
     float graph_dt = 0.0f, graph_speed = 0.0f;
+    // multigrid hierarchy of the mixed-precision solve (level 0 = the grid itself)
+    int mg_levels = 0;
+    void* mg_pool = nullptr;
+    MgLevel mg[kMaxMgLevels];
     // launch accounting and optional per-stage event timing
     long long launches = 0;
     float last_gpu_ms = 0.0f;
@@ -180,5 +193,8 @@ void launch_project(Env& e, float dtS);
 void launch_micro(Env& e, float dt, float speed);
 void launch_ground(Env& e, float dt, float speed, float irr);
 void launch_init_state(Env& e, int noise, uint32_t seed);
+bool mg_allocate(Env& e);
+void launch_matvec_textbook(Env& e, const float* s, float* As);
+void mg_solve(Env& e);
 
 }  // namespace skt

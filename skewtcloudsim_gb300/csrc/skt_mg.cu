@@ -1,0 +1,697 @@
+// Mixed-precision pressure solve: FP64 iterative refinement around an FP32 conjugate gradient
+// preconditioned by a geometric multigrid V-cycle.
+//
+// The reference's projection (calculatePressureProject, Game/environment.cu:898-987) runs a
+// Jacobi-preconditioned CG for at most 200 iterations, which at 512x256x512 leaves the residual
+// far above any tight tolerance. This solver uses the textbook (symmetric) operator A of the
+// projection and solves it to a relative FP64 residual of refine_tol:
+//
+//   x64 = 0
+//   repeat: r = b - A x64 (FP64 arithmetic, FP64 norm)    until |r|/|b| <= refine_tol
+//           solve A e = r with MG-PCG in FP32 (FP64 reductions) to |r_inner| <= inner_rtol |r|
+//           x64 += e
+//
+// Multigrid: cell-centred, the hierarchy of the full grid (ground cells inactive: diagonal 0).
+// Coarse face coefficient = 1/2 x (sum of the four fine coefficients of that face), the
+// boundary share of the diagonal coarsens the same way; damped Jacobi (omega 0.8), two pre- and
+// two post-sweeps, sum restriction, injection prolongation; the coarsest level (<= 4096 cells)
+// is relaxed in one block in shared memory. Equal pre/post smoothing keeps the preconditioner
+// symmetric, as CG needs. All levels keep A's sign convention: off-diagonal face coefficients
+// <= 0, diagonal = -(sum of the cell's six face coefficients) > 0 (symmetric positive definite).
+#include "skt_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace skt {
+
+namespace {
+
+constexpr float kOmega = 0.8f;
+constexpr int kCoarseMax = 4096;
+constexpr int kCoarseSweeps = 60;
+constexpr int MBX = 32, MBY = 8;
+
+struct LvlView {
+    int X, Y, Z;
+    const float *ax, *ay, *az, *aw;
+};
+
+__device__ __forceinline__ int lidx(const LvlView& L, int x, int y, int z) { return x + L.X * (y + L.Y * z); }
+
+// (A v)_c with zero values outside the grid; face coefficients of a cell's upper faces are
+// stored at the cell, the lower ones at the neighbour.
+__device__ __forceinline__ float apply_A(const LvlView& L, const float* __restrict__ v, int x, int y, int z, int c) {
+    float s = L.aw[c] * v[c];
+    if (x > 0) s += L.ax[c - 1] * v[c - 1];
+    if (x + 1 < L.X) s += L.ax[c] * v[c + 1];
+    if (y > 0) s += L.ay[c - L.X] * v[c - L.X];
+    if (y + 1 < L.Y) s += L.ay[c] * v[c + L.X];
+    const int XY = L.X * L.Y;
+    if (z > 0) s += L.az[c - XY] * v[c - XY];
+    if (z + 1 < L.Z) s += L.az[c] * v[c + XY];
+    return s;
+}
+
+inline dim3 lgrid(int X, int Y, int Z) { return dim3((X + MBX - 1) / MBX, (Y + MBY - 1) / MBY, Z); }
+
+// Coarse operator from the fine one. Interior faces only: a fine coefficient on a face leaving
+// the grid (possible on the finest level, where it carries the boundary share) counts as
+// boundary.
+__global__ void k_mg_coarsen(LvlView F, int CX, int CY, int CZ, float* __restrict__ cax, float* __restrict__ cay, float* __restrict__ caz,
+                             float* __restrict__ caw) {
+    const int I = blockIdx.x * MBX + threadIdx.x, J = blockIdx.y * MBY + threadIdx.y, K = blockIdx.z;
+    if (I >= CX || J >= CY) return;
+    const int XY = F.X * F.Y;
+    auto fax = [&](int x, int y, int z) { return (x >= 0 && x + 1 < F.X) ? F.ax[x + F.X * (y + F.Y * z)] : 0.0f; };
+    auto fay = [&](int x, int y, int z) { return (y >= 0 && y + 1 < F.Y) ? F.ay[x + F.X * (y + F.Y * z)] : 0.0f; };
+    auto faz = [&](int x, int y, int z) { return (z >= 0 && z + 1 < F.Z) ? F.az[x + F.X * (y + F.Y * z)] : 0.0f; };
+    float px = 0, mx = 0, py = 0, my = 0, pz = 0, mz = 0, E = 0;
+    for (int b = 0; b < 2; ++b)
+        for (int d = 0; d < 2; ++d) {
+            px += fax(2 * I + 1, 2 * J + b, 2 * K + d);
+            mx += fax(2 * I - 1, 2 * J + b, 2 * K + d);
+            py += fay(2 * I + b, 2 * J + 1, 2 * K + d);
+            my += fay(2 * I + b, 2 * J - 1, 2 * K + d);
+            pz += faz(2 * I + b, 2 * J + d, 2 * K + 1);
+            mz += faz(2 * I + b, 2 * J + d, 2 * K - 1);
+        }
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            for (int d = 0; d < 2; ++d) {
+                const int x = 2 * I + a, y = 2 * J + b, z = 2 * K + d;
+                const int c = x + F.X * (y + F.Y * z);
+                // diag = -(sum of the six face coefficients, boundary faces included), so the
+                // boundary share is diag + (sum of the interior-face coefficients) >= 0
+                const float interior = fax(x, y, z) + fax(x - 1, y, z) + fay(x, y, z) + fay(x, y - 1, z) + faz(x, y, z) + faz(x, y, z - 1);
+                E += F.aw[c] + interior;
+            }
+    (void)XY;
+    const int c = I + CX * (J + CY * K);
+    const float ax_ = 0.5f * px, ay_ = 0.5f * py, az_ = 0.5f * pz;
+    cax[c] = (I + 1 < CX) ? ax_ : 0.0f;
+    cay[c] = (J + 1 < CY) ? ay_ : 0.0f;
+    caz[c] = (K + 1 < CZ) ? az_ : 0.0f;
+    caw[c] = 0.5f * E - (0.5f * px + 0.5f * mx + 0.5f * py + 0.5f * my + 0.5f * pz + 0.5f * mz);
+}
+
+// damped Jacobi: out = in + omega (b - A in)/diag; first = true starts from in = 0
+template <bool FIRST>
+__global__ void k_mg_jacobi(LvlView L, const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ b) {
+    const int x = blockIdx.x * MBX + threadIdx.x, y = blockIdx.y * MBY + threadIdx.y, z = blockIdx.z;
+    if (x >= L.X || y >= L.Y) return;
+    const int c = lidx(L, x, y, z);
+    const float d = L.aw[c];
+    if (d == 0.0f) { out[c] = 0.0f; return; }
+    if (FIRST) out[c] = kOmega * b[c] / d;
+    else out[c] = in[c] + kOmega * (b[c] - apply_A(L, in, x, y, z, c)) / d;
+}
+
+// coarse right-hand side: the sum of the residuals of the eight children
+__global__ void k_mg_restrict(LvlView F, const float* __restrict__ x, const float* __restrict__ b, int CX, int CY, int CZ,
+                              float* __restrict__ cb) {
+    const int I = blockIdx.x * MBX + threadIdx.x, J = blockIdx.y * MBY + threadIdx.y, K = blockIdx.z;
+    if (I >= CX || J >= CY) return;
+    float s = 0.0f;
+    for (int d = 0; d < 2; ++d)
+        for (int bb = 0; bb < 2; ++bb)
+            for (int a = 0; a < 2; ++a) {
+                const int fx = 2 * I + a, fy = 2 * J + bb, fz = 2 * K + d;
+                const int c = lidx(F, fx, fy, fz);
+                if (F.aw[c] == 0.0f) continue;
+                s += b[c] - apply_A(F, x, fx, fy, fz, c);
+            }
+    cb[I + CX * (J + CY * K)] = s;
+}
+
+// x += P e (injection of the parent's correction)
+__global__ void k_mg_prolong(LvlView F, float* __restrict__ x, int CX, int CY, const float* __restrict__ ce) {
+    const int fx = blockIdx.x * MBX + threadIdx.x, fy = blockIdx.y * MBY + threadIdx.y, fz = blockIdx.z;
+    if (fx >= F.X || fy >= F.Y) return;
+    const int c = lidx(F, fx, fy, fz);
+    if (F.aw[c] == 0.0f) return;
+    x[c] += ce[(fx >> 1) + CX * ((fy >> 1) + CY * (fz >> 1))];
+}
+
+// the coarsest level: kCoarseSweeps damped Jacobi sweeps from zero in shared memory, one block
+__global__ void __launch_bounds__(512) k_mg_coarse(LvlView L, const float* __restrict__ b, float* __restrict__ x) {
+    extern __shared__ float sm[];
+    const int n = L.X * L.Y * L.Z;
+    float* xa = sm;
+    float* xb = sm + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xa[i] = 0.0f;
+    __syncthreads();
+    for (int it = 0; it < kCoarseSweeps; ++it) {
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            const int xx = c % L.X, yy = (c / L.X) % L.Y, zz = c / (L.X * L.Y);
+            const float d = L.aw[c];
+            xb[c] = d == 0.0f ? 0.0f : xa[c] + kOmega * (b[c] - apply_A(L, xa, xx, yy, zz, c)) / d;
+        }
+        __syncthreads();
+        float* t = xa; xa = xb; xb = t;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xa[i];
+}
+
+// ---- refinement / CG helpers (1D over all cells) ---------------------------------------------
+
+constexpr int RT = 256;
+
+template <int NTH>
+__device__ __forceinline__ double bsum(double v, double* sm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (NTH / 32) ? sm[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+template <int NTH>
+__device__ __forceinline__ float bmax(float v, float* sm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float t = 0.0f;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (NTH / 32) ? sm[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(0xffffffffu, t, o));
+    }
+    return t;
+}
+// last-block reduction of per-block (sum, max) partials; true in thread 0 of the last block
+__device__ __forceinline__ bool finish(Scalars* sc, double* partials, double sum, float mx, double& tot, float& mall) {
+    __shared__ bool last;
+    __shared__ double sd[RT / 32];
+    __shared__ float sf[RT / 32];
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = sum;
+        partials[kMaxPartials + blockIdx.x] = double(mx);
+        __threadfence();
+        last = atomicAdd(&sc->done_blocks, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    float m = 0.0f;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += RT) {
+        s += __ldcg(partials + b);
+        const float mb = float(__ldcg(partials + kMaxPartials + b));
+        m = mb > m ? mb : m;
+    }
+    const double ts = bsum<RT>(s, sd);
+    const float tm = bmax<RT>(m, sf);
+    if (threadIdx.x == 0) {
+        tot = ts;
+        mall = tm;
+        sc->done_blocks = 0;
+    }
+    return threadIdx.x == 0;
+}
+
+// r32 = b - A x64 in FP64, |r|^2 in FP64; mode 0 records |b|^2 (x64 = 0 on entry)
+__global__ void __launch_bounds__(RT) k_resid64(Grid g, const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ az,
+                                                const float* __restrict__ aw, const double* __restrict__ x, const float* __restrict__ b,
+                                                float* __restrict__ r, float refine_tol, int first, Scalars* sc, double* partials) {
+    __shared__ double smd[RT / 32];
+    double acc = 0.0;
+    float mx = 0.0f;
+    for (int c = blockIdx.x * RT + threadIdx.x; c < g.N; c += gridDim.x * RT) {
+        double rv = 0.0;
+        if (aw[c] != 0.0f) {
+            const int xx = c % g.X, yy = (c / g.X) % g.Y, zz = c / g.XY;
+            double s = double(aw[c]) * x[c];
+            if (xx > 0) s += double(ax[c - 1]) * x[c - 1];
+            if (xx + 1 < g.X) s += double(ax[c]) * x[c + 1];
+            if (yy > 0) s += double(ay[c - g.X]) * x[c - g.X];
+            if (yy + 1 < g.Y) s += double(ay[c]) * x[c + g.X];
+            if (zz > 0) s += double(az[c - g.XY]) * x[c - g.XY];
+            if (zz + 1 < g.Z) s += double(az[c]) * x[c + g.XY];
+            rv = double(b[c]) - s;
+        }
+        r[c] = float(rv);
+        acc += rv * rv;
+        const float m = fabsf(float(rv));
+        if (m > mx) mx = m;
+    }
+    const double bs = bsum<RT>(acc, smd);
+    double tot;
+    float mall;
+    if (finish(sc, partials, bs, mx, tot, mall)) {
+        if (first) sc->rnorm0 = sqrt(tot);
+        sc->rnorm = sqrt(tot);
+        sc->residual = mall;
+        const bool done = sc->rnorm0 == 0.0 || sc->rnorm <= double(refine_tol) * sc->rnorm0;
+        sc->refine_done = done ? 1 : 0;
+        sc->inner_tol = mall;       // the inner solves reduce the max residual relative to this
+    }
+}
+
+// x64 += e (FP64) and e = 0
+__global__ void __launch_bounds__(RT) k_accum64(int n, double* __restrict__ x, float* __restrict__ e) {
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) {
+        x[c] += double(e[c]);
+        e[c] = 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(RT) k_zero64(int n, double* __restrict__ x) {
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) x[c] = 0.0;
+}
+
+__global__ void __launch_bounds__(RT) k_cast64(int n, const double* __restrict__ x, float* __restrict__ p) {
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) p[c] = float(x[c]);
+}
+
+// inner CG: rho = z.r (FP64) and s = z (start), or beta = rho_new/rho and s = z + beta s
+template <bool START>
+__global__ void __launch_bounds__(RT) k_zr_search(int n, const float* __restrict__ z, const float* __restrict__ r, float* __restrict__ s,
+                                                  Scalars* sc, double* partials) {
+    if (!START && sc->converged) return;
+    // pass 1 of 2: the dot product; the search update runs in k_search_mg after beta is known
+    __shared__ double smd[RT / 32];
+    double acc = 0.0;
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) {
+        acc += double(z[c]) * double(r[c]);
+        if (START) s[c] = z[c];
+    }
+    const double bs = bsum<RT>(acc, smd);
+    double tot;
+    float mall;
+    if (finish(sc, partials, bs, 0.0f, tot, mall)) {
+        if (START) {
+            sc->sigma0 = tot;
+            sc->converged = 0;
+            sc->iters = 0;
+        } else {
+            sc->beta_f = float(tot / sc->sigma0);
+            sc->sigma0 = tot;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RT) k_search_mg(int n, const float* __restrict__ z, float* __restrict__ s, const Scalars* sc) {
+    if (sc->converged) return;
+    const float beta = sc->beta_f;
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) s[c] = z[c] + beta * s[c];
+}
+
+// As = A s and s.As -> alpha = rho / s.As
+__global__ void __launch_bounds__(RT) k_matvec_mg(Grid g, const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ az,
+                                                  const float* __restrict__ aw, const float* __restrict__ s, float* __restrict__ As,
+                                                  Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ double smd[RT / 32];
+    LvlView L{g.X, g.Y, g.Z, ax, ay, az, aw};
+    double acc = 0.0;
+    for (int c = blockIdx.x * RT + threadIdx.x; c < g.N; c += gridDim.x * RT) {
+        float v = 0.0f;
+        if (aw[c] != 0.0f) {
+            const int xx = c % g.X, yy = (c / g.X) % g.Y, zz = c / g.XY;
+            v = apply_A(L, s, xx, yy, zz, c);
+        }
+        As[c] = v;
+        acc += double(v) * double(s[c]);
+    }
+    const double bs = bsum<RT>(acc, smd);
+    double tot;
+    float mall;
+    if (finish(sc, partials, bs, 0.0f, tot, mall)) {
+        sc->sigma1 = tot;
+        sc->alpha = float(sc->sigma0 / tot);
+    }
+}
+
+// e += alpha s; r -= alpha As; stop when max|r| <= inner_rtol * (max residual at entry)
+__global__ void __launch_bounds__(RT) k_update_mg(int n, const float* __restrict__ s, const float* __restrict__ As, float* __restrict__ e,
+                                                  float* __restrict__ r, float inner_rtol, int max_iter, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ double smd[RT / 32];
+    __shared__ float smf[RT / 32];
+    const float alpha = sc->alpha;
+    float mx = 0.0f;
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) {
+        e[c] += alpha * s[c];
+        const float rv = r[c] - alpha * As[c];
+        r[c] = rv;
+        const float m = fabsf(rv);
+        if (m > mx) mx = m;
+    }
+    (void)smd;
+    const float bm = bmax<RT>(mx, smf);
+    double tot;
+    float mall;
+    if (finish(sc, partials, 0.0, bm, tot, mall)) {
+        sc->iters += 1;
+        sc->outer_inner_total += 1;
+        if (mall <= inner_rtol * sc->inner_tol) sc->converged = 1;
+        else if (sc->iters >= max_iter) sc->converged = 2;
+    }
+}
+
+// ---- vectorised finest level (X % 4 == 0) ---------------------------------------------------
+
+__device__ __forceinline__ float4 l4(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
+__device__ __forceinline__ void s4(float* p, int c, float4 v) { *reinterpret_cast<float4*>(p + c) = v; }
+
+constexpr int JVY = 4;
+
+// out = in + omega (b - A in)/diag as float4 with a z march (planes z-1, z, z+1 of `in` and the
+// previous plane's z coefficients in registers); inactive cells (diag 0) get 0
+__global__ void __launch_bounds__(32 * JVY) k_mg_jacobi4(Grid g, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
+                                                         const float* __restrict__ az, const float* __restrict__ aw,
+                                                         const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ b) {
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * JVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const int X = g.X, XY = g.XY;
+    const int row = x0 + y * X;
+    float4 vb = make_float4(0, 0, 0, 0), vc = vb, azb = vb;
+    if (act) {
+        vc = l4(in, row + zs * XY);
+        if (zs > 0) { vb = l4(in, row + (zs - 1) * XY); azb = l4(az, row + (zs - 1) * XY); }
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 vf = make_float4(0, 0, 0, 0), vd = vf, vu = vf, ayd = vf, cx = vf, cy = vf, cz = vf, cw = vf, bb = vf;
+        if (act) {
+            if (z + 1 < g.Z) vf = l4(in, c + XY);
+            if (y > 0) { vd = l4(in, c - X); ayd = l4(ay, c - X); }
+            if (y + 1 < g.Y) vu = l4(in, c + X);
+            cx = l4(ax, c); cy = l4(ay, c); cz = l4(az, c); cw = l4(aw, c); bb = l4(b, c);
+        }
+        float vl = __shfl_up_sync(0xffffffffu, vc.w, 1);
+        float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
+        float vr = __shfl_down_sync(0xffffffffu, vc.x, 1);
+        if (act && lane == 0) {
+            if (x0 > 0) { vl = in[c - 1]; axl = ax[c - 1]; } else { vl = 0.0f; axl = 0.0f; }
+        }
+        if (act && (lane == 31 || x0 + 4 >= X)) vr = (x0 + 4 < X) ? in[c + 4] : 0.0f;
+        if (act) {
+            const float a0 = cw.x * vc.x + axl * vl + ayd.x * vd.x + azb.x * vb.x + cx.x * vc.y + cy.x * vu.x + cz.x * vf.x;
+            const float a1 = cw.y * vc.y + cx.x * vc.x + ayd.y * vd.y + azb.y * vb.y + cx.y * vc.z + cy.y * vu.y + cz.y * vf.y;
+            const float a2 = cw.z * vc.z + cx.y * vc.y + ayd.z * vd.z + azb.z * vb.z + cx.z * vc.w + cy.z * vu.z + cz.z * vf.z;
+            const float a3 = cw.w * vc.w + cx.z * vc.z + ayd.w * vd.w + azb.w * vb.w + cx.w * vr + cy.w * vu.w + cz.w * vf.w;
+            float4 o;
+            o.x = cw.x == 0.0f ? 0.0f : vc.x + kOmega * (bb.x - a0) / cw.x;
+            o.y = cw.y == 0.0f ? 0.0f : vc.y + kOmega * (bb.y - a1) / cw.y;
+            o.z = cw.z == 0.0f ? 0.0f : vc.z + kOmega * (bb.z - a2) / cw.z;
+            o.w = cw.w == 0.0f ? 0.0f : vc.w + kOmega * (bb.w - a3) / cw.w;
+            s4(out, c, o);
+        }
+        vb = vc;
+        vc = vf;
+        azb = cz;
+    }
+}
+
+// out = omega b / diag (the first sweep from zero), float4 over all cells
+__global__ void __launch_bounds__(RT) k_mg_first4(int n4, const float4* __restrict__ aw, const float4* __restrict__ b, float4* __restrict__ out) {
+    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
+        const float4 d = aw[i], v = b[i];
+        float4 o;
+        o.x = d.x == 0.0f ? 0.0f : kOmega * v.x / d.x;
+        o.y = d.y == 0.0f ? 0.0f : kOmega * v.y / d.y;
+        o.z = d.z == 0.0f ? 0.0f : kOmega * v.z / d.z;
+        o.w = d.w == 0.0f ? 0.0f : kOmega * v.w / d.w;
+        out[i] = o;
+    }
+}
+
+// x += P e on the finest level, float4 (cells 4k..4k+3 have parents 2k and 2k+1 along x)
+__global__ void __launch_bounds__(RT) k_mg_prolong4(Grid g, int CX, int CY, const float* __restrict__ ce, const float* __restrict__ aw,
+                                                    float* __restrict__ x) {
+    const int n4 = g.N / 4, X4 = g.X / 4;
+    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
+        const int xq = i % X4, rest = i / X4;
+        const int y = rest % g.Y, z = rest / g.Y;
+        const int pbase = CX * ((y >> 1) + CY * (z >> 1));
+        const float e0 = ce[pbase + 2 * xq], e1 = ce[pbase + 2 * xq + 1];
+        const float4 d = *reinterpret_cast<const float4*>(aw + 4 * i);
+        float4 v = *reinterpret_cast<float4*>(x + 4 * i);
+        if (d.x != 0.0f) v.x += e0;
+        if (d.y != 0.0f) v.y += e0;
+        if (d.z != 0.0f) v.z += e1;
+        if (d.w != 0.0f) v.w += e1;
+        *reinterpret_cast<float4*>(x + 4 * i) = v;
+    }
+}
+
+// e += alpha s; r -= alpha As; inner stop on max|r|, float4
+__global__ void __launch_bounds__(RT) k_update_mg4(int n4, const float4* __restrict__ s, const float4* __restrict__ As, float4* __restrict__ e,
+                                                   float4* __restrict__ r, float inner_rtol, int max_iter, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ float smf[RT / 32];
+    const float alpha = sc->alpha;
+    float mx = 0.0f;
+    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
+        const float4 sv = s[i], av = As[i];
+        float4 ev = e[i], rv = r[i];
+        ev.x += alpha * sv.x; ev.y += alpha * sv.y; ev.z += alpha * sv.z; ev.w += alpha * sv.w;
+        rv.x = rv.x - alpha * av.x; rv.y = rv.y - alpha * av.y; rv.z = rv.z - alpha * av.z; rv.w = rv.w - alpha * av.w;
+        e[i] = ev;
+        r[i] = rv;
+        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(rv.x), fabsf(rv.y)), fmaxf(fabsf(rv.z), fabsf(rv.w))));
+    }
+    const float bm = bmax<RT>(mx, smf);
+    double tot;
+    float mall;
+    if (finish(sc, partials, 0.0, bm, tot, mall)) {
+        sc->iters += 1;
+        sc->outer_inner_total += 1;
+        if (mall <= inner_rtol * sc->inner_tol) sc->converged = 1;
+        else if (sc->iters >= max_iter) sc->converged = 2;
+    }
+}
+
+// rho = z.r (FP64 across threads); START also sets s = z
+template <bool START>
+__global__ void __launch_bounds__(RT) k_zr4(int n4, const float4* __restrict__ z, const float4* __restrict__ r, float4* __restrict__ s,
+                                            Scalars* sc, double* partials) {
+    if (!START && sc->converged) return;
+    __shared__ double smd[RT / 32];
+    float acc = 0.0f, comp = 0.0f;
+    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
+        const float4 zv = z[i], rv = r[i];
+        const float t = zv.x * rv.x + zv.y * rv.y + zv.z * rv.z + zv.w * rv.w;
+        const float yv = t - comp;
+        const float tt = acc + yv;
+        comp = (tt - acc) - yv;
+        acc = tt;
+        if (START) s[i] = zv;
+    }
+    const double bs = bsum<RT>(double(acc) - double(comp), smd);
+    double tot;
+    float mall;
+    if (finish(sc, partials, bs, 0.0f, tot, mall)) {
+        if (START) {
+            sc->sigma0 = tot;
+            sc->converged = 0;
+            sc->iters = 0;
+        } else {
+            sc->beta_f = float(tot / sc->sigma0);
+            sc->sigma0 = tot;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RT) k_search_mg4(int n4, const float4* __restrict__ z, float4* __restrict__ s, const Scalars* sc) {
+    if (sc->converged) return;
+    const float beta = sc->beta_f;
+    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
+        const float4 zv = z[i];
+        float4 sv = s[i];
+        sv.x = zv.x + beta * sv.x; sv.y = zv.y + beta * sv.y; sv.z = zv.z + beta * sv.z; sv.w = zv.w + beta * sv.w;
+        s[i] = sv;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------
+
+bool mg_allocate(Env& e) {
+    const Grid& g = e.g;
+    int X = g.X, Y = g.Y, Z = g.Z;
+    e.mg_levels = 0;
+    size_t bytes = 0;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    std::vector<int> dims;
+    dims.insert(dims.end(), {X, Y, Z});
+    while ((X % 2 == 0) && (Y % 2 == 0) && (Z % 2 == 0) && X * Y * Z > kCoarseMax && e.mg_levels + 1 < kMaxMgLevels) {
+        X /= 2; Y /= 2; Z /= 2;
+        dims.insert(dims.end(), {X, Y, Z});
+        bytes += al(size_t(X) * Y * Z * 4) * 7;
+        e.mg_levels++;
+    }
+    if (X * Y * Z > kCoarseMax) return false;  // no level small enough for the one-block solve
+    if (bytes && cudaMalloc(&e.mg_pool, bytes) != cudaSuccess) { cudaGetLastError(); return false; }
+    char* p = (char*)e.mg_pool;
+    for (int l = 0; l <= e.mg_levels; ++l) {
+        MgLevel& L = e.mg[l];
+        L.X = dims[3 * l]; L.Y = dims[3 * l + 1]; L.Z = dims[3 * l + 2];
+        if (l == 0) continue;
+        const size_t n = size_t(L.X) * L.Y * L.Z;
+        float** arr[7] = {&L.ax, &L.ay, &L.az, &L.aw, &L.x, &L.x2, &L.b};
+        for (auto a : arr) { *a = (float*)p; p += al(n * 4); }
+    }
+    return true;
+}
+
+namespace {
+
+LvlView view(Env& e, int l) {
+    if (l == 0) return LvlView{e.g.X, e.g.Y, e.g.Z, e.ax, e.ay, e.az, e.aw};
+    const MgLevel& L = e.mg[l];
+    return LvlView{L.X, L.Y, L.Z, L.ax, L.ay, L.az, L.aw};
+}
+
+void mg_setup(Env& e) {
+    for (int l = 0; l < e.mg_levels; ++l) {
+        const MgLevel& C = e.mg[l + 1];
+        k_mg_coarsen<<<lgrid(C.X, C.Y, C.Z), dim3(MBX, MBY), 0, e.stream>>>(view(e, l), C.X, C.Y, C.Z, C.ax, C.ay, C.az, C.aw);
+        e.launches += 1;
+    }
+}
+
+// z = V(b) on level l (level 0: x = z0, x2 = z0b)
+void vcycle(Env& e, int l, const float* b, float* x, float* x2) {
+    const LvlView L = view(e, l);
+    if (l == e.mg_levels) {
+        const int n = L.X * L.Y * L.Z;
+        k_mg_coarse<<<1, 512, 2 * n * sizeof(float), e.stream>>>(L, b, x);
+        e.launches += 1;
+        return;
+    }
+    const dim3 gr = lgrid(L.X, L.Y, L.Z), bl(MBX, MBY);
+    MgLevel& C = e.mg[l + 1];
+    if (l == 0 && (e.g.X % 4) == 0) {
+        const Grid& g = e.g;
+        const int n4 = g.N / 4;
+        const int ns = std::min((n4 + RT - 1) / RT, e.num_sms * 8);
+        const int gx = (g.X / 4 + 31) / 32, gy = (g.Y + JVY - 1) / JVY;
+        int zc = std::max(1, std::min(g.Z, (e.num_sms * 12 + gx * gy - 1) / (gx * gy)));
+        const int zlen = (g.Z + zc - 1) / zc;
+        zc = (g.Z + zlen - 1) / zlen;
+        const dim3 jg(gx, gy, zc), jb(32, JVY);
+        k_mg_first4<<<ns, RT, 0, e.stream>>>(n4, (const float4*)e.aw, (const float4*)b, (float4*)x2);
+        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, x, b);
+        k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b);
+        vcycle(e, l + 1, C.b, C.x, C.x2);
+        k_mg_prolong4<<<ns, RT, 0, e.stream>>>(g, C.X, C.Y, C.x, e.aw, x);
+        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x, x2, b);
+        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, x, b);
+        e.launches += 6;
+        return;
+    }
+    k_mg_jacobi<true><<<gr, bl, 0, e.stream>>>(L, nullptr, x2, b);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, b);
+    k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b);
+    vcycle(e, l + 1, C.b, C.x, C.x2);
+    k_mg_prolong<<<gr, bl, 0, e.stream>>>(L, x, C.X, C.Y, C.x);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x, x2, b);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, b);
+    e.launches += 6;
+}
+
+}  // namespace
+
+// Solves A p = b (b = the divergence in e.r on entry, A from k_build in textbook form) into
+// e.pp. Uses e.tA (b), e.tB (inner correction), e.r/e.s/e.As (inner CG) and e.rd (V-cycle
+// vectors). Returns after the refinement met refine_tol or the outer cap.
+void mg_solve(Env& e) {
+    const Grid& g = e.g;
+    const int n = g.N;
+    const int nb = std::min((n + RT - 1) / RT, std::min(e.num_sms * 8, kMaxPartials));
+    float* bvec = e.tA;
+    float* ecor = e.tB;
+    float* z0 = (float*)e.rd;
+    float* z0b = z0 + size_t(n);
+    {
+        ProfScope ps(e, "mg_setup");
+        mg_setup(e);
+        cudaMemcpyAsync(bvec, e.r, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, e.stream);
+        cudaMemsetAsync(ecor, 0, sizeof(float) * size_t(n), e.stream);
+        k_zero64<<<nb, RT, 0, e.stream>>>(n, e.xd);
+        cudaMemsetAsync(&e.sc->outer_inner_total, 0, sizeof(int), e.stream);
+        e.launches += 1;
+    }
+    int outer = 0;
+    const int max_outer = 12;
+    for (; outer < max_outer; ++outer) {
+        {
+            ProfScope ps(e, "mg_refine");
+            k_resid64<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, e.xd, bvec, e.r, e.cfg.refine_tol, outer == 0, e.sc, e.partials);
+            e.launches += 1;
+        }
+        cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
+        cudaStreamSynchronize(e.stream);
+        if (e.host_sc->refine_done == 1) break;
+        // inner MG-PCG on A e = r
+        {
+            ProfScope ps(e, "mg_vcycle");
+            vcycle(e, 0, e.r, z0, z0b);
+        }
+        const bool vec = (g.X % 4) == 0;
+        const int n4 = n / 4;
+        if (vec) k_zr4<true><<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (const float4*)e.r, (float4*)e.s, e.sc, e.partials);
+        else k_zr_search<true><<<nb, RT, 0, e.stream>>>(n, z0, e.r, e.s, e.sc, e.partials);
+        e.launches += 1;
+        const int chunk = 4;
+        for (int it = 0; it < e.cfg.inner_max_iter; it += chunk) {
+            for (int k = 0; k < chunk && it + k < e.cfg.inner_max_iter; ++k) {
+                if (vec) {
+                    { ProfScope ps(e, "mg_matvec"); launch_matvec_textbook(e, e.s, e.As); }
+                    { ProfScope ps(e, "mg_update");
+                      k_update_mg4<<<nb, RT, 0, e.stream>>>(n4, (const float4*)e.s, (const float4*)e.As, (float4*)ecor, (float4*)e.r,
+                                                           e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials); }
+                    { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b); }
+                    { ProfScope ps(e, "mg_search");
+                      k_zr4<false><<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (const float4*)e.r, nullptr, e.sc, e.partials);
+                      k_search_mg4<<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (float4*)e.s, e.sc); }
+                    e.launches += 3;
+                    continue;
+                }
+                { ProfScope ps(e, "mg_matvec");
+                  k_matvec_mg<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, e.s, e.As, e.sc, e.partials); }
+                { ProfScope ps(e, "mg_update");
+                  k_update_mg<<<nb, RT, 0, e.stream>>>(n, e.s, e.As, ecor, e.r, e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials); }
+                { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b); }
+                { ProfScope ps(e, "mg_search");
+                  k_zr_search<false><<<nb, RT, 0, e.stream>>>(n, z0, e.r, e.s, e.sc, e.partials);
+                  k_search_mg<<<nb, RT, 0, e.stream>>>(n, z0, e.s, e.sc); }
+                e.launches += 4;
+            }
+            cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
+            cudaStreamSynchronize(e.stream);
+            if (e.host_sc->converged) break;
+        }
+        { ProfScope ps(e, "mg_refine");
+          k_accum64<<<nb, RT, 0, e.stream>>>(n, e.xd, ecor);
+          e.launches += 1; }
+    }
+    k_cast64<<<nb, RT, 0, e.stream>>>(n, e.xd, e.pp);
+    e.launches += 1;
+    cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    e.last_outer = outer;
+    e.last_iters = e.host_sc->outer_inner_total;
+    e.last_residual = float(e.host_sc->rnorm0 > 0 ? e.host_sc->rnorm / e.host_sc->rnorm0 : 0.0);
+    e.last_converged = e.host_sc->refine_done == 1;
+}
+
+}  // namespace skt

@@ -61,33 +61,9 @@ __device__ __forceinline__ float block_max(float v, float* sm) {
     return t;
 }
 
-// Publishes one block partial (sum, max) and returns true in thread 0 of the last block to
-// finish, which then sees every partial. Partials are summed in block order: deterministic.
-__device__ __forceinline__ bool publish(Scalars* sc, double* partials, double sum, float mx, double& tot, float& mxall) {
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = sum;
-        partials[kMaxPartials + blockIdx.x] = double(mx);
-        __threadfence();
-        const unsigned t = atomicAdd(&sc->done_blocks, 1u);
-        last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!last) return false;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        double s = 0.0, m = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) {
-            s += ((volatile double*)partials)[b];
-            const double mb = ((volatile double*)partials)[kMaxPartials + b];
-            m = mb > m ? mb : m;
-        }
-        tot = s;
-        mxall = float(m);
-        sc->done_blocks = 0;
-    }
-    return threadIdx.x == 0;
-}
+// Publishes one block partial (sum, max) of a 1D NT-thread grid; thread 0 of the last block to
+// finish gets the totals (see publish_n). Defined after the generic reductions below.
+__device__ __forceinline__ bool publish(Scalars* sc, double* partials, double sum, float mx, double& tot, float& mxall);
 
 __device__ __forceinline__ float char_trunc(float a) {  // (char) of a float: truncate, saturate (Q3)
     const float t = truncf(a);
@@ -333,10 +309,15 @@ __device__ __forceinline__ float block_max_n(float v, float* sm, int tid) {
     }
     return t;
 }
-// publish() for any grid shape: bid = linear block id, nb = number of blocks
+// publish() for any grid shape: bid = linear block id, nb = number of blocks. The last block to
+// finish reduces all partials with every thread (fixed assignment, fixed tree): deterministic.
+// Returns true in thread 0 of that block, with tot/mxall set.
+template <int NTH>
 __device__ __forceinline__ bool publish_n(Scalars* sc, double* partials, int bid, int nb, int tid, double sum, float mx, double& tot,
                                           float& mxall) {
     __shared__ bool last;
+    __shared__ double sms[NTH / 32];
+    __shared__ float smm[NTH / 32];
     if (tid == 0) {
         partials[bid] = sum;
         partials[kMaxPartials + bid] = double(mx);
@@ -346,19 +327,26 @@ __device__ __forceinline__ bool publish_n(Scalars* sc, double* partials, int bid
     }
     __syncthreads();
     if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    float m = 0.0f;
+    for (int b = tid; b < nb; b += NTH) {
+        s += __ldcg(partials + b);
+        const float mb = float(__ldcg(partials + kMaxPartials + b));
+        m = mb > m ? mb : m;
+    }
+    const double ts = block_sum_n<NTH>(s, sms, tid);
+    const float tm = block_max_n<NTH>(m, smm, tid);
     if (tid == 0) {
-        __threadfence();
-        double s = 0.0, m = 0.0;
-        for (int b = 0; b < nb; ++b) {
-            s += ((volatile double*)partials)[b];
-            const double mb = ((volatile double*)partials)[kMaxPartials + b];
-            m = mb > m ? mb : m;
-        }
-        tot = s;
-        mxall = float(m);
+        tot = ts;
+        mxall = tm;
         sc->done_blocks = 0;
     }
     return tid == 0;
+}
+
+__device__ __forceinline__ bool publish(Scalars* sc, double* partials, double sum, float mx, double& tot, float& mxall) {
+    return publish_n<NT>(sc, partials, blockIdx.x, gridDim.x, threadIdx.x, sum, mx, tot, mxall);
 }
 
 constexpr int UT = 256;
@@ -398,7 +386,7 @@ __global__ void __launch_bounds__(UT) k_update4(int n4, int xy4, const float4* _
     const float bm = block_max_n<UT>(mx, smf, threadIdx.x);
     double tot;
     float mall;
-    if (publish_n(sc, partials, blockIdx.x, gridDim.x, threadIdx.x, bs, bm, tot, mall)) {
+    if (publish_n<UT>(sc, partials, blockIdx.x, gridDim.x, threadIdx.x, bs, bm, tot, mall)) {
         sc->iters += 1;
         sc->residual = mall;
         if (mall <= tol) {
@@ -509,7 +497,7 @@ __global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* 
     const int nb = gridDim.x * gridDim.y * gridDim.z;
     double tot;
     float mall;
-    if (publish_n(sc, partials, bid, nb, tid, bs, 0.0f, tot, mall)) {
+    if (publish_n<MVT>(sc, partials, bid, nb, tid, bs, 0.0f, tot, mall)) {
         const double s1 = reference ? sc->sigma1 + tot : tot;
         sc->sigma1 = s1;
         sc->alpha = float(sc->sigma0 / s1);
@@ -555,6 +543,19 @@ __global__ void __launch_bounds__(256) k_apply_proj(Grid g, const float* __restr
 
 }  // namespace
 
+// As = A s and s.As -> alpha (textbook operator, vectorised; X % 4 == 0)
+void launch_matvec_textbook(Env& e, const float* s, float* As) {
+    const Grid& g = e.g;
+    const dim3 mvb(32, MVY);
+    const int gx = (g.X / 4 + 31) / 32, gy = (g.Y + MVY - 1) / MVY;
+    int zc = std::max(1, std::min(g.Z, (e.num_sms * 8 + gx * gy - 1) / (gx * gy)));
+    while (gx * gy * zc > kMaxPartials && zc > 1) --zc;
+    const int zlen = (g.Z + zc - 1) / zc;
+    zc = (g.Z + zlen - 1) / zlen;
+    k_matvec4<<<dim3(gx, gy, zc), mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, s, As, 0, e.sc, e.partials);
+    e.launches += 1;
+}
+
 void launch_project(Env& e, float dtS) {
     const Grid& g = e.g;
     const Tiles T = tiles_of(g);
@@ -567,6 +568,9 @@ void launch_project(Env& e, float dtS) {
     k_build<<<nblk, NT, 0, e.stream>>>(g, T, e.rho, e.u, e.v, e.w, e.defU, e.defW, dtS, e.ax, e.ay, e.az, e.aw, e.r, e.s, e.pp, e.As, ref,
                                       e.sc, e.partials);
     }
+    if (e.cfg.precision == 1) {
+        mg_solve(e);
+    } else {
     const int chunk = 8;
     const bool vec = (g.X % 4) == 0;
     // vectorised launch shapes: streams at 8 blocks/SM, the matvec's z chunks sized to fill the GPU
@@ -603,6 +607,7 @@ void launch_project(Env& e, float dtS) {
     e.last_iters = e.host_sc->iters;
     e.last_residual = e.host_sc->residual;
     e.last_converged = e.host_sc->converged == 1;
+    }
     const dim3 grd((g.X + 31) / 32, (g.Y + 7) / 8, g.Z), blk(32, 8);
     ProfScope ps(e, "proj_apply");
     e.launches += 2;

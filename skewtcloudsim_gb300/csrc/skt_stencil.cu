@@ -215,8 +215,12 @@ __global__ void __launch_bounds__(256) k_ppm(Grid g, const float* __restrict__ i
 
 // One cell of a directional PPM pass from its 5-value windows (q and the density companion):
 // the same arithmetic as k_ppm.
+// When the companion's window is all ones its reconstruction is exactly 1 (the slope, limiter and
+// parabola terms all vanish), so its face fluxes are exactly the face velocities; the two
+// ppm_flux calls are skipped with a bit-identical result.
 __device__ __forceinline__ float ppm_cell(const float* q, const float* o, float vc, float vm, float dt, float vox) {
     float nq, nr;
+    const bool ones = o[0] == 1.0f && o[1] == 1.0f && o[3] == 1.0f && o[4] == 1.0f;
     {
         float L, C, R;
         if (vc >= 0.0f) { L = q[1]; C = q[2]; R = q[3]; } else { L = q[4]; C = q[3]; R = q[2]; }
@@ -225,7 +229,9 @@ __device__ __forceinline__ float ppm_cell(const float* q, const float* o, float 
         const float fm = ppm_flux(vm, L, C, R, dt, vox);
         nq = q[2] - (dt / vox) * (fp - fm);
     }
-    {
+    if (ones) {
+        nr = 1.0f - (dt / vox) * (vc - vm);
+    } else {
         float L, C, R;
         if (vc >= 0.0f) { L = o[1]; C = o[2]; R = o[3]; } else { L = o[4]; C = o[3]; R = o[2]; }
         const float fp = ppm_flux(vc, L, C, R, dt, vox);
@@ -403,6 +409,39 @@ __global__ void __launch_bounds__(256) k_maxvel(Grid g, const float* __restrict_
         if (t > m) m = t;
     }
     if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(&sc->maxbits, __float_as_uint(m));
+}
+
+// flat terrain: the same max over rows y >= 1, as float4 streams with one atomic per block
+__global__ void __launch_bounds__(256) k_maxvel4(int n4, int X4, int Y, int XY4, const float4* __restrict__ a0, const float4* __restrict__ a1,
+                                                 const float4* __restrict__ a2, int reference, Scalars* __restrict__ sc) {
+    __shared__ float sm[8];
+    float m = 0.0f;
+    for (int i = blockIdx.x * 256 + threadIdx.x; i < n4; i += gridDim.x * 256) {
+        if ((i / X4) % Y == 0) continue;  // the ground layer
+        const bool absv = !reference || i < XY4;
+        const float4 v[3] = {a0[i], a1[i], a2[i]};
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float e0 = v[j].x, e1 = v[j].y, e2 = v[j].z, e3 = v[j].w;
+            if (absv) { e0 = fabsf(e0); e1 = fabsf(e1); e2 = fabsf(e2); e3 = fabsf(e3); }
+            if (e0 > m) m = e0;
+            if (e1 > m) m = e1;
+            if (e2 > m) m = e2;
+            if (e3 > m) m = e3;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float t = __shfl_xor_sync(0xffffffffu, m, o);
+        if (t > m) m = t;
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = 0.0f;
+        for (int w = 0; w < 8; ++w) b = sm[w] > b ? sm[w] : b;
+        if (b > 0.0f) atomicMax(&sc->maxbits, __float_as_uint(b));
+    }
 }
 
 // Courant substeps from the max velocity, on the device (Game/environment.cu:726-730)
@@ -605,7 +644,14 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     ProfScope ps(e, "advect");
     e.launches += 2;
     cudaMemsetAsync(&e.sc->maxbits, 0, sizeof(unsigned int), e.stream);
-    k_maxvel<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, e.u, e.v, e.w, e.cfg.semantics == 0, e.sc);
+    if (e.flat && (g.X % 4) == 0) {
+        const int n4 = g.N / 4;
+        k_maxvel4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, g.XY / 4, (const float4*)e.u,
+                                                                                  (const float4*)e.v, (const float4*)e.w,
+                                                                                  e.cfg.semantics == 0, e.sc);
+    } else {
+        k_maxvel<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, e.u, e.v, e.w, e.cfg.semantics == 0, e.sc);
+    }
     k_nsub<<<1, 1, 0, e.stream>>>(e.sc, dtS, g.vox, float(e.cfg.max_substeps));
     int nsub = -1;
     int slots;
