@@ -157,7 +157,7 @@ void skt_default_config(skt_solver_cfg* c) {
     c->precision = SKT_PCG_PLAIN;
     c->refine_tol = 1e-8f;
     c->inner_max_iter = 60;
-    c->inner_rtol = 1e-3f;
+    c->inner_rtol = 1e-4f;
     c->use_graph = 0;
 }
 

@@ -13,9 +13,9 @@
 //
 // Multigrid: cell-centred, the hierarchy of the full grid (ground cells inactive: diagonal 0).
 // Coarse face coefficient = 1/2 x (sum of the four fine coefficients of that face), the
-// boundary share of the diagonal coarsens the same way; damped Jacobi (omega 0.8), two pre- and
-// two post-sweeps, sum restriction, injection prolongation; the coarsest level (<= 4096 cells)
-// is relaxed in one block in shared memory. Equal pre/post smoothing keeps the preconditioner
+// boundary share of the diagonal coarsens the same way; a degree-2 Chebyshev smoother before
+// and after the coarse correction, sum restriction, injection prolongation; the coarsest level
+// (<= 4096 cells) is relaxed in one block in shared memory. Equal pre/post smoothing keeps the preconditioner
 // symmetric, as CG needs. All levels keep A's sign convention: off-diagonal face coefficients
 // <= 0, diagonal = -(sum of the cell's six face coefficients) > 0 (symmetric positive definite).
 #include "skt_internal.cuh"
@@ -28,7 +28,16 @@ namespace skt {
 
 namespace {
 
-constexpr float kOmega = 0.8f;
+constexpr float kOmega = 0.8f;  // damped Jacobi weight of the coarsest-level relaxation
+// Degree-2 Chebyshev smoother on D^-1 A over [lmax/8, 1.05 lmax], lmax = 2 (D^-1 A of this
+// diagonally dominant M-matrix has its spectrum in (0, 2]):
+//   step A: x1 = x0 + (b - A x0)/(theta D)
+//   step B: x2 = x1 + c1 (x1 - x0) + c2 (b - A x1)/D
+// From x0 = 0 step A is x1 = b/(theta D). Pre- and post-smoothing use the same polynomial, so
+// the V-cycle stays symmetric.
+constexpr float kChebTheta = 1.175f;                 // (2.1 + 0.25)/2
+constexpr float kChebC1 = 0.44900f;                  // rho1 rho0
+constexpr float kChebC2 = 1.23319f;                  // 2 rho1 / delta
 constexpr int kCoarseMax = 4096;
 constexpr int kCoarseSweeps = 60;
 constexpr int MBX = 32, MBY = 8;
@@ -96,16 +105,20 @@ __global__ void k_mg_coarsen(LvlView F, int CX, int CY, int CZ, float* __restric
     caw[c] = 0.5f * E - (0.5f * px + 0.5f * mx + 0.5f * py + 0.5f * my + 0.5f * pz + 0.5f * mz);
 }
 
-// damped Jacobi: out = in + omega (b - A in)/diag; first = true starts from in = 0
+// one smoother step: out = in + c1 (in - prev) + c2 (b - A in)/diag (prev may be null = 0);
+// FIRST: out = b/(theta diag) (step A from zero). Inactive cells (diag 0) get 0.
 template <bool FIRST>
-__global__ void k_mg_jacobi(LvlView L, const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ b) {
+__global__ void k_mg_jacobi(LvlView L, const float* __restrict__ in, const float* __restrict__ prev, float* __restrict__ out,
+                            const float* __restrict__ b, float c1, float c2) {
     const int x = blockIdx.x * MBX + threadIdx.x, y = blockIdx.y * MBY + threadIdx.y, z = blockIdx.z;
     if (x >= L.X || y >= L.Y) return;
     const int c = lidx(L, x, y, z);
     const float d = L.aw[c];
     if (d == 0.0f) { out[c] = 0.0f; return; }
-    if (FIRST) out[c] = kOmega * b[c] / d;
-    else out[c] = in[c] + kOmega * (b[c] - apply_A(L, in, x, y, z, c)) / d;
+    if (FIRST) { out[c] = b[c] / (kChebTheta * d); return; }
+    const float v = in[c];
+    const float pv = prev ? prev[c] : 0.0f;
+    out[c] = v + c1 * (v - pv) + c2 * (b[c] - apply_A(L, in, x, y, z, c)) / d;
 }
 
 // coarse right-hand side: the sum of the residuals of the eight children
@@ -366,11 +379,13 @@ __device__ __forceinline__ void s4(float* p, int c, float4 v) { *reinterpret_cas
 
 constexpr int JVY = 4;
 
-// out = in + omega (b - A in)/diag as float4 with a z march (planes z-1, z, z+1 of `in` and the
-// previous plane's z coefficients in registers); inactive cells (diag 0) get 0
+// one smoother step out = in + c1 (in - prev) + c2 (b - A in)/diag as float4 with a z march
+// (planes z-1, z, z+1 of `in` and the previous plane's z coefficients in registers); prev may
+// be null (= 0) and may alias out (read before the write of the same cell); inactive cells get 0
 __global__ void __launch_bounds__(32 * JVY) k_mg_jacobi4(Grid g, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
                                                          const float* __restrict__ az, const float* __restrict__ aw,
-                                                         const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ b) {
+                                                         const float* __restrict__ in, const float* prev, float* out,
+                                                         const float* __restrict__ b, float c1, float c2) {
     const int lane = threadIdx.x;
     const int x0 = (blockIdx.x * 32 + lane) * 4;
     const int y = blockIdx.y * JVY + threadIdx.y;
@@ -404,11 +419,12 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_jacobi4(Grid g, int zlen, const
             const float a1 = cw.y * vc.y + cx.x * vc.x + ayd.y * vd.y + azb.y * vb.y + cx.y * vc.z + cy.y * vu.y + cz.y * vf.y;
             const float a2 = cw.z * vc.z + cx.y * vc.y + ayd.z * vd.z + azb.z * vb.z + cx.z * vc.w + cy.z * vu.z + cz.z * vf.z;
             const float a3 = cw.w * vc.w + cx.z * vc.z + ayd.w * vd.w + azb.w * vb.w + cx.w * vr + cy.w * vu.w + cz.w * vf.w;
+            const float4 pv = prev ? l4(prev, c) : make_float4(0, 0, 0, 0);
             float4 o;
-            o.x = cw.x == 0.0f ? 0.0f : vc.x + kOmega * (bb.x - a0) / cw.x;
-            o.y = cw.y == 0.0f ? 0.0f : vc.y + kOmega * (bb.y - a1) / cw.y;
-            o.z = cw.z == 0.0f ? 0.0f : vc.z + kOmega * (bb.z - a2) / cw.z;
-            o.w = cw.w == 0.0f ? 0.0f : vc.w + kOmega * (bb.w - a3) / cw.w;
+            o.x = cw.x == 0.0f ? 0.0f : vc.x + c1 * (vc.x - pv.x) + c2 * (bb.x - a0) / cw.x;
+            o.y = cw.y == 0.0f ? 0.0f : vc.y + c1 * (vc.y - pv.y) + c2 * (bb.y - a1) / cw.y;
+            o.z = cw.z == 0.0f ? 0.0f : vc.z + c1 * (vc.z - pv.z) + c2 * (bb.z - a2) / cw.z;
+            o.w = cw.w == 0.0f ? 0.0f : vc.w + c1 * (vc.w - pv.w) + c2 * (bb.w - a3) / cw.w;
             s4(out, c, o);
         }
         vb = vc;
@@ -417,15 +433,15 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_jacobi4(Grid g, int zlen, const
     }
 }
 
-// out = omega b / diag (the first sweep from zero), float4 over all cells
+// out = b / (theta diag) (smoother step A from zero), float4 over all cells
 __global__ void __launch_bounds__(RT) k_mg_first4(int n4, const float4* __restrict__ aw, const float4* __restrict__ b, float4* __restrict__ out) {
     for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
         const float4 d = aw[i], v = b[i];
         float4 o;
-        o.x = d.x == 0.0f ? 0.0f : kOmega * v.x / d.x;
-        o.y = d.y == 0.0f ? 0.0f : kOmega * v.y / d.y;
-        o.z = d.z == 0.0f ? 0.0f : kOmega * v.z / d.z;
-        o.w = d.w == 0.0f ? 0.0f : kOmega * v.w / d.w;
+        o.x = d.x == 0.0f ? 0.0f : v.x / (kChebTheta * d.x);
+        o.y = d.y == 0.0f ? 0.0f : v.y / (kChebTheta * d.y);
+        o.z = d.z == 0.0f ? 0.0f : v.z / (kChebTheta * d.z);
+        o.w = d.w == 0.0f ? 0.0f : v.w / (kChebTheta * d.w);
         out[i] = o;
     }
 }
@@ -579,6 +595,7 @@ void vcycle(Env& e, int l, const float* b, float* x, float* x2) {
     }
     const dim3 gr = lgrid(L.X, L.Y, L.Z), bl(MBX, MBY);
     MgLevel& C = e.mg[l + 1];
+    const float c2a = 1.0f / kChebTheta;
     if (l == 0 && (e.g.X % 4) == 0) {
         const Grid& g = e.g;
         const int n4 = g.N / 4;
@@ -588,23 +605,25 @@ void vcycle(Env& e, int l, const float* b, float* x, float* x2) {
         const int zlen = (g.Z + zc - 1) / zc;
         zc = (g.Z + zlen - 1) / zlen;
         const dim3 jg(gx, gy, zc), jb(32, JVY);
+        // pre-smoothing from zero: A -> x2, B -> x
         k_mg_first4<<<ns, RT, 0, e.stream>>>(n4, (const float4*)e.aw, (const float4*)b, (float4*)x2);
-        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, x, b);
+        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, nullptr, x, b, kChebC1, kChebC2);
         k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b);
         vcycle(e, l + 1, C.b, C.x, C.x2);
         k_mg_prolong4<<<ns, RT, 0, e.stream>>>(g, C.X, C.Y, C.x, e.aw, x);
-        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x, x2, b);
-        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, x, b);
+        // post-smoothing: A x -> x2, B (x2, prev x) -> x
+        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x, nullptr, x2, b, 0.0f, c2a);
+        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, x, x, b, kChebC1, kChebC2);
         e.launches += 6;
         return;
     }
-    k_mg_jacobi<true><<<gr, bl, 0, e.stream>>>(L, nullptr, x2, b);
-    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, b);
+    k_mg_jacobi<true><<<gr, bl, 0, e.stream>>>(L, nullptr, nullptr, x2, b, 0.0f, 0.0f);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, nullptr, x, b, kChebC1, kChebC2);
     k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b);
     vcycle(e, l + 1, C.b, C.x, C.x2);
     k_mg_prolong<<<gr, bl, 0, e.stream>>>(L, x, C.X, C.Y, C.x);
-    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x, x2, b);
-    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, b);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x, nullptr, x2, b, 0.0f, c2a);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, x, b, kChebC1, kChebC2);
     e.launches += 6;
 }
 

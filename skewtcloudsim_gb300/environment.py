@@ -100,7 +100,7 @@ class SolverConfig:
     precision: int = 0          # 0 plain, 1 mixed
     refine_tol: float = 1e-8
     inner_max_iter: int = 60
-    inner_rtol: float = 1e-3
+    inner_rtol: float = 1e-4
     use_graph: int = 0
 
     def c(self):
