@@ -182,6 +182,7 @@ def main():
     ap.add_argument("--workload", default="precision-512x512x256")
     ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
     ap.add_argument("--semantics", type=int, default=0)
+    ap.add_argument("--mg-half", type=int, default=1, help="mixed: FP16 finest-level coefficients in the V-cycle")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--shape", default=None, help="x,y,z (z vertical) override of the workload size")
@@ -202,7 +203,7 @@ def main():
 
     shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
     init, dt, speed = sounding.workload(args.workload, scale=shape)
-    cfg = SolverConfig(semantics=args.semantics, precision=1 if args.mode == "mixed" else 0)
+    cfg = SolverConfig(semantics=args.semantics, precision=1 if args.mode == "mixed" else 0, mg_half=args.mg_half)
     env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
     env.init_from(init)
     cells = init.nx * init.ny * init.nz

@@ -79,6 +79,7 @@ typedef struct {
     int inner_max_iter; /* MIXED: FP32 iterations per refinement step */
     float inner_rtol;   /* MIXED: relative tolerance of each FP32 inner solve */
     int use_graph;      /* capture the step in a CUDA graph (substep slots = max_substeps) */
+    int mg_half;        /* MIXED: the V-cycle smooths with FP16 copies of the finest coefficients */
 } skt_solver_cfg;
 
 typedef struct {

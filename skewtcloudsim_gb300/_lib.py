@@ -21,7 +21,7 @@ class SolverCfg(ctypes.Structure):
     _fields_ = [("semantics", ctypes.c_int), ("diffuse_sweeps", ctypes.c_int), ("pcg_tol", ctypes.c_float),
                 ("pcg_max_iter", ctypes.c_int), ("max_substeps", ctypes.c_int), ("precision", ctypes.c_int),
                 ("refine_tol", ctypes.c_float), ("inner_max_iter", ctypes.c_int), ("inner_rtol", ctypes.c_float),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("mg_half", ctypes.c_int)]
 
 
 class StepStats(ctypes.Structure):

@@ -159,6 +159,7 @@ void skt_default_config(skt_solver_cfg* c) {
     c->inner_max_iter = 60;
     c->inner_rtol = 1e-4f;
     c->use_graph = 0;
+    c->mg_half = 1;
 }
 
 const char* skt_version(void) { return "skewt-gb300 0.1 (sm_103a)"; }
@@ -189,7 +190,7 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     e.g.N = int(n);
     e.g.vox = grid->voxel;
     e.cfg = SolverCfg{c.semantics, c.diffuse_sweeps, c.pcg_tol, c.pcg_max_iter, c.max_substeps, c.precision, c.refine_tol, c.inner_max_iter,
-                      c.inner_rtol, c.use_graph};
+                      c.inner_rtol, c.use_graph, c.mg_half};
     const size_t N = size_t(n), NG = size_t(grid->nx) * grid->nz, NY = size_t(grid->ny);
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const int nsky = 12 + 2 + 4 + 4;

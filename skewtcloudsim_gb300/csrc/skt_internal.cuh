@@ -104,6 +104,7 @@ struct SolverCfg {
     int inner_max_iter;
     float inner_rtol;
     int use_graph;
+    int mg_half;         // mixed: FP16 finest-level coefficients in the V-cycle
 };
 
 struct Env {
@@ -154,6 +155,7 @@ struct Env {
     int mg_levels = 0;
     void* mg_pool = nullptr;
     MgLevel mg[kMaxMgLevels];
+    void* mg_h = nullptr;         // FP16 ax, ay, az, aw of the finest level (4 x N halves, in mg_pool)
     // launch accounting and optional per-stage event timing
     long long launches = 0;
     float last_gpu_ms = 0.0f;

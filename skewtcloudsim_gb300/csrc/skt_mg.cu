@@ -20,6 +20,8 @@
 // <= 0, diagonal = -(sum of the cell's six face coefficients) > 0 (symmetric positive definite).
 #include "skt_internal.cuh"
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -109,7 +111,8 @@ __global__ void k_mg_coarsen(LvlView F, int CX, int CY, int CZ, float* __restric
 // FIRST: out = b/(theta diag) (step A from zero). Inactive cells (diag 0) get 0.
 template <bool FIRST>
 __global__ void k_mg_jacobi(LvlView L, const float* __restrict__ in, const float* __restrict__ prev, float* __restrict__ out,
-                            const float* __restrict__ b, float c1, float c2) {
+                            const float* __restrict__ b, float c1, float c2, const int* skip) {
+    if (skip && *skip) return;
     const int x = blockIdx.x * MBX + threadIdx.x, y = blockIdx.y * MBY + threadIdx.y, z = blockIdx.z;
     if (x >= L.X || y >= L.Y) return;
     const int c = lidx(L, x, y, z);
@@ -123,7 +126,8 @@ __global__ void k_mg_jacobi(LvlView L, const float* __restrict__ in, const float
 
 // coarse right-hand side: the sum of the residuals of the eight children
 __global__ void k_mg_restrict(LvlView F, const float* __restrict__ x, const float* __restrict__ b, int CX, int CY, int CZ,
-                              float* __restrict__ cb) {
+                              float* __restrict__ cb, const int* skip) {
+    if (skip && *skip) return;
     const int I = blockIdx.x * MBX + threadIdx.x, J = blockIdx.y * MBY + threadIdx.y, K = blockIdx.z;
     if (I >= CX || J >= CY) return;
     float s = 0.0f;
@@ -139,7 +143,8 @@ __global__ void k_mg_restrict(LvlView F, const float* __restrict__ x, const floa
 }
 
 // x += P e (injection of the parent's correction)
-__global__ void k_mg_prolong(LvlView F, float* __restrict__ x, int CX, int CY, const float* __restrict__ ce) {
+__global__ void k_mg_prolong(LvlView F, float* __restrict__ x, int CX, int CY, const float* __restrict__ ce, const int* skip) {
+    if (skip && *skip) return;
     const int fx = blockIdx.x * MBX + threadIdx.x, fy = blockIdx.y * MBY + threadIdx.y, fz = blockIdx.z;
     if (fx >= F.X || fy >= F.Y) return;
     const int c = lidx(F, fx, fy, fz);
@@ -148,7 +153,8 @@ __global__ void k_mg_prolong(LvlView F, float* __restrict__ x, int CX, int CY, c
 }
 
 // the coarsest level: kCoarseSweeps damped Jacobi sweeps from zero in shared memory, one block
-__global__ void __launch_bounds__(512) k_mg_coarse(LvlView L, const float* __restrict__ b, float* __restrict__ x) {
+__global__ void __launch_bounds__(512) k_mg_coarse(LvlView L, const float* __restrict__ b, float* __restrict__ x, const int* skip) {
+    if (skip && *skip) return;
     extern __shared__ float sm[];
     const int n = L.X * L.Y * L.Z;
     float* xa = sm;
@@ -349,7 +355,6 @@ __global__ void __launch_bounds__(RT) k_matvec_mg(Grid g, const float* __restric
 __global__ void __launch_bounds__(RT) k_update_mg(int n, const float* __restrict__ s, const float* __restrict__ As, float* __restrict__ e,
                                                   float* __restrict__ r, float inner_rtol, int max_iter, Scalars* sc, double* partials) {
     if (sc->converged) return;
-    __shared__ double smd[RT / 32];
     __shared__ float smf[RT / 32];
     const float alpha = sc->alpha;
     float mx = 0.0f;
@@ -360,7 +365,6 @@ __global__ void __launch_bounds__(RT) k_update_mg(int n, const float* __restrict
         const float m = fabsf(rv);
         if (m > mx) mx = m;
     }
-    (void)smd;
     const float bm = bmax<RT>(mx, smf);
     double tot;
     float mall;
@@ -372,60 +376,251 @@ __global__ void __launch_bounds__(RT) k_update_mg(int n, const float* __restrict
     }
 }
 
-// ---- vectorised finest level (X % 4 == 0) ---------------------------------------------------
-
-__device__ __forceinline__ float4 l4(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
-__device__ __forceinline__ void s4(float* p, int c, float4 v) { *reinterpret_cast<float4*>(p + c) = v; }
+// ---- vector levels (X % 4 == 0) -------------------------------------------------------------
 
 constexpr int JVY = 4;
 
-// one smoother step out = in + c1 (in - prev) + c2 (b - A in)/diag as float4 with a z march
-// (planes z-1, z, z+1 of `in` and the previous plane's z coefficients in registers); prev may
-// be null (= 0) and may alias out (read before the write of the same cell); inactive cells get 0
-__global__ void __launch_bounds__(32 * JVY) k_mg_jacobi4(Grid g, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
-                                                         const float* __restrict__ az, const float* __restrict__ aw,
-                                                         const float* __restrict__ in, const float* prev, float* out,
-                                                         const float* __restrict__ b, float c1, float c2) {
-    const int lane = threadIdx.x;
+// The vector levels (X % 4 == 0) run every V-cycle step as one float4 z march: a thread owns
+// four consecutive x cells of one (y) row and walks a run of z planes, keeping the input vector
+// of planes z-1, z, z+1 and the back-face coefficients in registers. Neighbouring rows come from
+// the block's other warps through L1, the x edges from the lanes beside it (warp shuffles).
+// Coefficients are FP32 or, on the finest level, FP16 copies (4 halves = 8 bytes per 4 cells).
+
+__device__ __forceinline__ float4 ld4(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
+struct alignas(8) H4 { __half2 a, b; };
+__device__ __forceinline__ float4 ld4(const __half* p, int c) {
+    const H4 h = *reinterpret_cast<const H4*>(p + c);
+    const float2 a = __half22float2(h.a), b = __half22float2(h.b);
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ float ld1(const float* p, int c) { return p[c]; }
+__device__ __forceinline__ float ld1(const __half* p, int c) { return __half2float(p[c]); }
+
+enum { SM_PRE = 0, SM_POSTA = 1, SM_POSTB = 2 };
+enum { DOT_NONE = 0, DOT_START = 1, DOT_NEXT = 2 };
+
+// The smoother's input vector u as seen by the stencil:
+//   SM_PRE   u = b / (theta diag)       (step A of the Chebyshev smoother from zero, on the fly)
+//   SM_POSTA u = x + P e_coarse         (the coarse correction, injected on the fly)
+//   SM_POSTB u = x2                     (the output of step A)
+// Values at inactive cells do not matter: every face coefficient that touches an inactive cell
+// is 0 on every level (ground faces have coefficient 0 and coarsening sums them).
+template <int MODE, class CT>
+struct UIn {
+    const float* v;
+    const CT* aw;
+    const float* ce;
+    int CX, CY;
+    __device__ __forceinline__ float4 row(int c, int x0, int y, int z) const {
+        const float4 a = ld4(v, c);
+        if (MODE == SM_PRE) {
+            const float4 d = ld4(aw, c);
+            return make_float4(d.x == 0.0f ? 0.0f : a.x / (kChebTheta * d.x), d.y == 0.0f ? 0.0f : a.y / (kChebTheta * d.y),
+                               d.z == 0.0f ? 0.0f : a.z / (kChebTheta * d.z), d.w == 0.0f ? 0.0f : a.w / (kChebTheta * d.w));
+        }
+        if (MODE == SM_POSTA) {
+            const float2 e = *reinterpret_cast<const float2*>(ce + (x0 >> 1) + CX * ((y >> 1) + CY * (z >> 1)));
+            return make_float4(a.x + e.x, a.y + e.x, a.z + e.y, a.w + e.y);
+        }
+        return a;
+    }
+    __device__ __forceinline__ float one(int c, int xx, int y, int z) const {
+        const float a = v[c];
+        if (MODE == SM_PRE) {
+            const float d = ld1(aw, c);
+            return d == 0.0f ? 0.0f : a / (kChebTheta * d);
+        }
+        if (MODE == SM_POSTA) return a + ce[(xx >> 1) + CX * ((y >> 1) + CY * (z >> 1))];
+        return a;
+    }
+};
+
+// block-wide sum over NTH threads with a linear thread id; the total is valid in tid 0
+template <int NTH>
+__device__ __forceinline__ double bsum_t(double v, double* sm, int tid) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((tid & 31) == 0) sm[tid >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (tid < 32) {
+        t = tid < (NTH / 32) ? sm[tid] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+// last-block reduction of one FP64 partial per block of a 3D grid; true in tid 0 of the last block
+template <int NTH>
+__device__ __forceinline__ bool finish_sum(Scalars* sc, double* partials, double sum, double& tot, int tid) {
+    __shared__ bool last;
+    __shared__ double sd[NTH / 32];
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nblk = gridDim.x * gridDim.y * gridDim.z;
+    if (tid == 0) {
+        partials[bid] = sum;
+        __threadfence();
+        last = atomicAdd(&sc->done_blocks, 1u) == unsigned(nblk) - 1u;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    for (int b = tid; b < nblk; b += NTH) s += __ldcg(partials + b);
+    const double ts = bsum_t<NTH>(s, sd, tid);
+    if (tid == 0) {
+        tot = ts;
+        sc->done_blocks = 0;
+    }
+    return tid == 0;
+}
+
+// (A u) at the four cells of a row from the z-march registers
+struct Stencil4 {
+    float4 a;
+    __device__ __forceinline__ Stencil4(float4 cw, float4 cx, float4 cy, float4 ayd, float4 azb, float4 cz, float axl, float4 vc,
+                                        float vl, float vr, float4 vd, float4 vu, float4 vb, float4 vf) {
+        a.x = cw.x * vc.x + axl * vl + ayd.x * vd.x + azb.x * vb.x + cx.x * vc.y + cy.x * vu.x + cz.x * vf.x;
+        a.y = cw.y * vc.y + cx.x * vc.x + ayd.y * vd.y + azb.y * vb.y + cx.y * vc.z + cy.y * vu.y + cz.y * vf.y;
+        a.z = cw.z * vc.z + cx.y * vc.y + ayd.z * vd.z + azb.z * vb.z + cx.z * vc.w + cy.z * vu.z + cz.z * vf.z;
+        a.w = cw.w * vc.w + cx.z * vc.z + ayd.w * vd.w + azb.w * vb.w + cx.w * vr + cy.w * vu.w + cz.w * vf.w;
+    }
+};
+
+// One smoother step out = u + k1 (u - prev) + k2 (b - A u)/diag on a vector level (inactive
+// cells get 0), u per MODE (see UIn); prev = 0 for SM_PRE (the step from zero), x + P e for
+// SM_POSTB, unused for SM_POSTA (k1 = 0). SM_POSTB may write over x (prev is read at the cell
+// being written only). DOT forms z.r (r = b) of the finest level's output for the CG:
+// DOT_START sets sigma0 and restarts the iteration count, DOT_NEXT sets beta = rho_new/rho.
+template <int MODE, int DOT, class CT>
+__global__ void __launch_bounds__(32 * JVY) k_mg_smooth4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
+                                                         const CT* __restrict__ az, const CT* __restrict__ aw, const float* __restrict__ b,
+                                                         UIn<MODE, CT> U, UIn<SM_POSTA, CT> Pv, float* out, float k1, float k2,
+                                                         const int* skip, Scalars* sc, double* partials) {
+    if (skip && *skip) return;
+    const int lane = threadIdx.x, tid = threadIdx.x + 32 * threadIdx.y;
     const int x0 = (blockIdx.x * 32 + lane) * 4;
     const int y = blockIdx.y * JVY + threadIdx.y;
-    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
-    const bool act = x0 < g.X && y < g.Y;
-    const int X = g.X, XY = g.XY;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, Z);
+    const bool act = x0 < X && y < Y;
+    const int XY = X * Y;
     const int row = x0 + y * X;
-    float4 vb = make_float4(0, 0, 0, 0), vc = vb, azb = vb;
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    float4 vb = z4, vc = z4, azb = z4;
     if (act) {
-        vc = l4(in, row + zs * XY);
-        if (zs > 0) { vb = l4(in, row + (zs - 1) * XY); azb = l4(az, row + (zs - 1) * XY); }
+        vc = U.row(row + zs * XY, x0, y, zs);
+        if (zs > 0) { vb = U.row(row + (zs - 1) * XY, x0, y, zs - 1); azb = ld4(az, row + (zs - 1) * XY); }
     }
+    float acc = 0.0f, comp = 0.0f;
     for (int z = zs; z < ze; ++z) {
         const int c = row + z * XY;
-        float4 vf = make_float4(0, 0, 0, 0), vd = vf, vu = vf, ayd = vf, cx = vf, cy = vf, cz = vf, cw = vf, bb = vf;
+        float4 vf = z4, vd = z4, vu = z4, ayd = z4, cx = z4, cy = z4, cz = z4, cw = z4, bb = z4;
         if (act) {
-            if (z + 1 < g.Z) vf = l4(in, c + XY);
-            if (y > 0) { vd = l4(in, c - X); ayd = l4(ay, c - X); }
-            if (y + 1 < g.Y) vu = l4(in, c + X);
-            cx = l4(ax, c); cy = l4(ay, c); cz = l4(az, c); cw = l4(aw, c); bb = l4(b, c);
+            if (z + 1 < Z) vf = U.row(c + XY, x0, y, z + 1);
+            if (y > 0) { vd = U.row(c - X, x0, y - 1, z); ayd = ld4(ay, c - X); }
+            if (y + 1 < Y) vu = U.row(c + X, x0, y + 1, z);
+            cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c); bb = ld4(b, c);
         }
         float vl = __shfl_up_sync(0xffffffffu, vc.w, 1);
         float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
         float vr = __shfl_down_sync(0xffffffffu, vc.x, 1);
         if (act && lane == 0) {
-            if (x0 > 0) { vl = in[c - 1]; axl = ax[c - 1]; } else { vl = 0.0f; axl = 0.0f; }
+            if (x0 > 0) { vl = U.one(c - 1, x0 - 1, y, z); axl = ld1(ax, c - 1); } else { vl = 0.0f; axl = 0.0f; }
         }
-        if (act && (lane == 31 || x0 + 4 >= X)) vr = (x0 + 4 < X) ? in[c + 4] : 0.0f;
+        if (act && (lane == 31 || x0 + 4 >= X)) vr = (x0 + 4 < X) ? U.one(c + 4, x0 + 4, y, z) : 0.0f;
         if (act) {
-            const float a0 = cw.x * vc.x + axl * vl + ayd.x * vd.x + azb.x * vb.x + cx.x * vc.y + cy.x * vu.x + cz.x * vf.x;
-            const float a1 = cw.y * vc.y + cx.x * vc.x + ayd.y * vd.y + azb.y * vb.y + cx.y * vc.z + cy.y * vu.y + cz.y * vf.y;
-            const float a2 = cw.z * vc.z + cx.y * vc.y + ayd.z * vd.z + azb.z * vb.z + cx.z * vc.w + cy.z * vu.z + cz.z * vf.z;
-            const float a3 = cw.w * vc.w + cx.z * vc.z + ayd.w * vd.w + azb.w * vb.w + cx.w * vr + cy.w * vu.w + cz.w * vf.w;
-            const float4 pv = prev ? l4(prev, c) : make_float4(0, 0, 0, 0);
+            const float4 a = Stencil4(cw, cx, cy, ayd, azb, cz, axl, vc, vl, vr, vd, vu, vb, vf).a;
+            const float4 pv = MODE == SM_POSTB ? Pv.row(c, x0, y, z) : z4;
             float4 o;
-            o.x = cw.x == 0.0f ? 0.0f : vc.x + c1 * (vc.x - pv.x) + c2 * (bb.x - a0) / cw.x;
-            o.y = cw.y == 0.0f ? 0.0f : vc.y + c1 * (vc.y - pv.y) + c2 * (bb.y - a1) / cw.y;
-            o.z = cw.z == 0.0f ? 0.0f : vc.z + c1 * (vc.z - pv.z) + c2 * (bb.z - a2) / cw.z;
-            o.w = cw.w == 0.0f ? 0.0f : vc.w + c1 * (vc.w - pv.w) + c2 * (bb.w - a3) / cw.w;
-            s4(out, c, o);
+            o.x = cw.x == 0.0f ? 0.0f : vc.x + k1 * (vc.x - pv.x) + k2 * (bb.x - a.x) / cw.x;
+            o.y = cw.y == 0.0f ? 0.0f : vc.y + k1 * (vc.y - pv.y) + k2 * (bb.y - a.y) / cw.y;
+            o.z = cw.z == 0.0f ? 0.0f : vc.z + k1 * (vc.z - pv.z) + k2 * (bb.z - a.z) / cw.z;
+            o.w = cw.w == 0.0f ? 0.0f : vc.w + k1 * (vc.w - pv.w) + k2 * (bb.w - a.w) / cw.w;
+            *reinterpret_cast<float4*>(out + c) = o;
+            if (DOT != DOT_NONE) {
+                const float t = o.x * bb.x + o.y * bb.y + o.z * bb.z + o.w * bb.w;
+                const float yv = t - comp;
+                const float tt = acc + yv;
+                comp = (tt - acc) - yv;
+                acc = tt;
+            }
+        }
+        vb = vc;
+        vc = vf;
+        azb = cz;
+    }
+    if (DOT != DOT_NONE) {
+        __shared__ double smd[JVY];
+        const double bs = bsum_t<32 * JVY>(double(acc) - double(comp), smd, tid);
+        double tot;
+        if (finish_sum<32 * JVY>(sc, partials, bs, tot, tid)) {
+            if (DOT == DOT_START) {
+                sc->sigma0 = tot;
+                sc->beta_f = 0.0f;
+                sc->converged = 0;
+                sc->iters = 0;
+            } else {
+                sc->beta_f = float(tot / sc->sigma0);
+                sc->sigma0 = tot;
+            }
+        }
+    }
+}
+
+// Coarse right-hand side of a vector level: each coarse cell gets the sum of b - A x over its
+// eight children. zlen, the z offset of every block, Y and JVY are even: a thread sums its row's
+// x pairs over two planes, then the even row of each row pair adds its partner's sums.
+template <class CT>
+__global__ void __launch_bounds__(32 * JVY) k_mg_restrict4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
+                                                           const CT* __restrict__ az, const CT* __restrict__ aw, const float* __restrict__ x,
+                                                           const float* __restrict__ b, int CX, int CY, float* __restrict__ cb, const int* skip) {
+    if (skip && *skip) return;
+    __shared__ float2 part[JVY][32];
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * JVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, Z);
+    const bool act = x0 < X && y < Y;
+    const int XY = X * Y;
+    const int row = x0 + y * X;
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    float4 vb = z4, vc = z4, azb = z4;
+    if (act) {
+        vc = ld4(x, row + zs * XY);
+        if (zs > 0) { vb = ld4(x, row + (zs - 1) * XY); azb = ld4(az, row + (zs - 1) * XY); }
+    }
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 vf = z4, vd = z4, vu = z4, ayd = z4, cx = z4, cy = z4, cz = z4, cw = z4, bb = z4;
+        if (act) {
+            if (z + 1 < Z) vf = ld4(x, c + XY);
+            if (y > 0) { vd = ld4(x, c - X); ayd = ld4(ay, c - X); }
+            if (y + 1 < Y) vu = ld4(x, c + X);
+            cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c); bb = ld4(b, c);
+        }
+        float vl = __shfl_up_sync(0xffffffffu, vc.w, 1);
+        float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
+        float vr = __shfl_down_sync(0xffffffffu, vc.x, 1);
+        if (act && lane == 0) {
+            if (x0 > 0) { vl = x[c - 1]; axl = ld1(ax, c - 1); } else { vl = 0.0f; axl = 0.0f; }
+        }
+        if (act && (lane == 31 || x0 + 4 >= X)) vr = (x0 + 4 < X) ? x[c + 4] : 0.0f;
+        if (act) {
+            const float4 a = Stencil4(cw, cx, cy, ayd, azb, cz, axl, vc, vl, vr, vd, vu, vb, vf).a;
+            acc.x += (cw.x == 0.0f ? 0.0f : bb.x - a.x) + (cw.y == 0.0f ? 0.0f : bb.y - a.y);
+            acc.y += (cw.z == 0.0f ? 0.0f : bb.z - a.z) + (cw.w == 0.0f ? 0.0f : bb.w - a.w);
+        }
+        if (z & 1) {
+            part[threadIdx.y][lane] = acc;
+            __syncthreads();
+            if (act && (threadIdx.y & 1) == 0) {
+                const float2 o = part[threadIdx.y + 1][lane];
+                *reinterpret_cast<float2*>(cb + (x0 >> 1) + CX * ((y >> 1) + CY * (z >> 1))) = make_float2(acc.x + o.x, acc.y + o.y);
+            }
+            __syncthreads();
+            acc = make_float2(0.0f, 0.0f);
         }
         vb = vc;
         vc = vf;
@@ -433,35 +628,109 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_jacobi4(Grid g, int zlen, const
     }
 }
 
-// out = b / (theta diag) (smoother step A from zero), float4 over all cells
-__global__ void __launch_bounds__(RT) k_mg_first4(int n4, const float4* __restrict__ aw, const float4* __restrict__ b, float4* __restrict__ out) {
-    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
-        const float4 d = aw[i], v = b[i];
-        float4 o;
-        o.x = d.x == 0.0f ? 0.0f : v.x / (kChebTheta * d.x);
-        o.y = d.y == 0.0f ? 0.0f : v.y / (kChebTheta * d.y);
-        o.z = d.z == 0.0f ? 0.0f : v.z / (kChebTheta * d.z);
-        o.w = d.w == 0.0f ? 0.0f : v.w / (kChebTheta * d.w);
-        out[i] = o;
+// CG search step fused with the operator: s_new = z + beta s_old (beta = 0: s_new = z, s_old
+// is not read), As = A s_new with the FP32 finest coefficients, s_new.As -> alpha = rho/(s.As)
+__global__ void __launch_bounds__(32 * JVY) k_mg_matvec_search4(int X, int Y, int Z, int zlen, const float* __restrict__ ax,
+                                                                const float* __restrict__ ay, const float* __restrict__ az,
+                                                                const float* __restrict__ aw, const float* __restrict__ zv,
+                                                                const float* __restrict__ sold, float* __restrict__ snew,
+                                                                float* __restrict__ As, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    const float beta = sc->beta_f;
+    const bool old = beta != 0.0f;
+    const int lane = threadIdx.x, tid = threadIdx.x + 32 * threadIdx.y;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * JVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, Z);
+    const bool act = x0 < X && y < Y;
+    const int XY = X * Y;
+    const int row = x0 + y * X;
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    auto srow = [&](int c) {
+        float4 v = ld4(zv, c);
+        if (old) {
+            const float4 s = ld4(sold, c);
+            v.x += beta * s.x; v.y += beta * s.y; v.z += beta * s.z; v.w += beta * s.w;
+        }
+        return v;
+    };
+    auto sone = [&](int c) { return old ? zv[c] + beta * sold[c] : zv[c]; };
+    float4 vb = z4, vc = z4, azb = z4;
+    if (act) {
+        vc = srow(row + zs * XY);
+        if (zs > 0) { vb = srow(row + (zs - 1) * XY); azb = ld4(az, row + (zs - 1) * XY); }
+    }
+    float acc = 0.0f, comp = 0.0f;
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 vf = z4, vd = z4, vu = z4, ayd = z4, cx = z4, cy = z4, cz = z4, cw = z4;
+        if (act) {
+            if (z + 1 < Z) vf = srow(c + XY);
+            if (y > 0) { vd = srow(c - X); ayd = ld4(ay, c - X); }
+            if (y + 1 < Y) vu = srow(c + X);
+            cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c);
+        }
+        float vl = __shfl_up_sync(0xffffffffu, vc.w, 1);
+        float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
+        float vr = __shfl_down_sync(0xffffffffu, vc.x, 1);
+        if (act && lane == 0) {
+            if (x0 > 0) { vl = sone(c - 1); axl = ax[c - 1]; } else { vl = 0.0f; axl = 0.0f; }
+        }
+        if (act && (lane == 31 || x0 + 4 >= X)) vr = (x0 + 4 < X) ? sone(c + 4) : 0.0f;
+        if (act) {
+            float4 a = Stencil4(cw, cx, cy, ayd, azb, cz, axl, vc, vl, vr, vd, vu, vb, vf).a;
+            if (cw.x == 0.0f) a.x = 0.0f;
+            if (cw.y == 0.0f) a.y = 0.0f;
+            if (cw.z == 0.0f) a.z = 0.0f;
+            if (cw.w == 0.0f) a.w = 0.0f;
+            *reinterpret_cast<float4*>(snew + c) = vc;
+            *reinterpret_cast<float4*>(As + c) = a;
+            const float t = a.x * vc.x + a.y * vc.y + a.z * vc.z + a.w * vc.w;
+            const float yv = t - comp;
+            const float tt = acc + yv;
+            comp = (tt - acc) - yv;
+            acc = tt;
+        }
+        vb = vc;
+        vc = vf;
+        azb = cz;
+    }
+    __shared__ double smd[JVY];
+    const double bs = bsum_t<32 * JVY>(double(acc) - double(comp), smd, tid);
+    double tot;
+    if (finish_sum<32 * JVY>(sc, partials, bs, tot, tid)) {
+        sc->sigma1 = tot;
+        sc->alpha = float(sc->sigma0 / tot);
     }
 }
 
-// x += P e on the finest level, float4 (cells 4k..4k+3 have parents 2k and 2k+1 along x)
-__global__ void __launch_bounds__(RT) k_mg_prolong4(Grid g, int CX, int CY, const float* __restrict__ ce, const float* __restrict__ aw,
-                                                    float* __restrict__ x) {
-    const int n4 = g.N / 4, X4 = g.X / 4;
-    for (int i = blockIdx.x * RT + threadIdx.x; i < n4; i += gridDim.x * RT) {
-        const int xq = i % X4, rest = i / X4;
-        const int y = rest % g.Y, z = rest / g.Y;
-        const int pbase = CX * ((y >> 1) + CY * (z >> 1));
-        const float e0 = ce[pbase + 2 * xq], e1 = ce[pbase + 2 * xq + 1];
-        const float4 d = *reinterpret_cast<const float4*>(aw + 4 * i);
-        float4 v = *reinterpret_cast<float4*>(x + 4 * i);
-        if (d.x != 0.0f) v.x += e0;
-        if (d.y != 0.0f) v.y += e0;
-        if (d.z != 0.0f) v.z += e1;
-        if (d.w != 0.0f) v.w += e1;
-        *reinterpret_cast<float4*>(x + 4 * i) = v;
+// FP16 copies of the finest level's coefficients for the V-cycle. Faces round toward zero; the
+// diagonal is the sum of the cell's rounded interior faces plus its FP32 boundary share, rounded
+// up, so every row keeps A's weak diagonal dominance and the smoothed operator stays symmetric
+// positive definite. Inactive cells keep diagonal 0.
+__global__ void __launch_bounds__(RT) k_mg_half(Grid g, const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ az,
+                                                const float* __restrict__ aw, __half* __restrict__ hx, __half* __restrict__ hy,
+                                                __half* __restrict__ hz, __half* __restrict__ hw) {
+    for (int c = blockIdx.x * RT + threadIdx.x; c < g.N; c += gridDim.x * RT) {
+        const __half fx = __float2half_ru(ax[c]), fy = __float2half_ru(ay[c]), fz = __float2half_ru(az[c]);
+        hx[c] = fx;
+        hy[c] = fy;
+        hz[c] = fz;
+        const float d = aw[c];
+        if (d == 0.0f) { hw[c] = __float2half(0.0f); continue; }
+        const int xx = c % g.X, yy = (c / g.X) % g.Y, zz = c / g.XY;
+        float s = 0.0f, sh = 0.0f;
+        auto face = [&](bool inner, float a, __half h) {
+            if (inner) { s -= a; sh -= __half2float(h); }
+        };
+        face(xx + 1 < g.X, ax[c], fx);
+        face(xx > 0, xx > 0 ? ax[c - 1] : 0.0f, __float2half_ru(xx > 0 ? ax[c - 1] : 0.0f));
+        face(yy + 1 < g.Y, ay[c], fy);
+        face(yy > 0, yy > 0 ? ay[c - g.X] : 0.0f, __float2half_ru(yy > 0 ? ay[c - g.X] : 0.0f));
+        face(zz + 1 < g.Z, az[c], fz);
+        face(zz > 0, zz > 0 ? az[c - g.XY] : 0.0f, __float2half_ru(zz > 0 ? az[c - g.XY] : 0.0f));
+        const float share = fmaxf(d - s, 0.0f);
+        hw[c] = __float2half_ru(sh + share);
     }
 }
 
@@ -555,8 +824,12 @@ bool mg_allocate(Env& e) {
         e.mg_levels++;
     }
     if (X * Y * Z > kCoarseMax) return false;  // no level small enough for the one-block solve
-    if (bytes && cudaMalloc(&e.mg_pool, bytes) != cudaSuccess) { cudaGetLastError(); return false; }
+    const size_t hbytes = al(size_t(g.N) * 2) * 4;
+    bytes += hbytes;
+    if (cudaMalloc(&e.mg_pool, bytes) != cudaSuccess) { cudaGetLastError(); return false; }
     char* p = (char*)e.mg_pool;
+    e.mg_h = p;
+    p += hbytes;
     for (int l = 0; l <= e.mg_levels; ++l) {
         MgLevel& L = e.mg[l];
         L.X = dims[3 * l]; L.Y = dims[3 * l + 1]; L.Z = dims[3 * l + 2];
@@ -576,55 +849,123 @@ LvlView view(Env& e, int l) {
     return LvlView{L.X, L.Y, L.Z, L.ax, L.ay, L.az, L.aw};
 }
 
+// the four FP16 coefficient arrays of the finest level (256-byte aligned, in mg_pool)
+void half_arrays(const Env& e, __half* h[4]) {
+    const size_t stride = (size_t(e.g.N) * 2 + 255) / 256 * 128;
+    for (int k = 0; k < 4; ++k) h[k] = (__half*)e.mg_h + k * stride;
+}
+
+bool vec_level(const Env& e, int l);
+
 void mg_setup(Env& e) {
     for (int l = 0; l < e.mg_levels; ++l) {
         const MgLevel& C = e.mg[l + 1];
         k_mg_coarsen<<<lgrid(C.X, C.Y, C.Z), dim3(MBX, MBY), 0, e.stream>>>(view(e, l), C.X, C.Y, C.Z, C.ax, C.ay, C.az, C.aw);
         e.launches += 1;
     }
+    if (e.cfg.mg_half && vec_level(e, 0)) {
+        __half* h[4];
+        half_arrays(e, h);
+        const int nb = std::min((e.g.N + RT - 1) / RT, e.num_sms * 8);
+        k_mg_half<<<nb, RT, 0, e.stream>>>(e.g, e.ax, e.ay, e.az, e.aw, h[0], h[1], h[2], h[3]);
+        e.launches += 1;
+    }
 }
 
-// z = V(b) on level l (level 0: x = z0, x2 = z0b)
-void vcycle(Env& e, int l, const float* b, float* x, float* x2) {
+// z-march launch shape of a vector level: about 12 blocks of 32 x JVY threads per SM, at most
+// kMaxPartials blocks (the fused dot products keep one partial per block), even plane runs
+struct March {
+    dim3 grid;
+    int zlen;
+};
+March march(const Env& e, int X, int Y, int Z) {
+    const int gx = (X / 4 + 31) / 32, gy = (Y + JVY - 1) / JVY;
+    int zc = std::max(1, std::min(Z, (e.num_sms * 12 + gx * gy - 1) / (gx * gy)));
+    zc = std::max(1, std::min(zc, kMaxPartials / (gx * gy)));
+    int zlen = (Z + zc - 1) / zc;
+    zlen += zlen & 1;
+    zc = (Z + zlen - 1) / zlen;
+    return {dim3(gx, gy, zc), zlen};
+}
+
+// A level runs the float4 kernels when its x size is a multiple of 4; the finest level also
+// needs its z-march grid to fit the partial slots of the fused dot product.
+bool vec_level(const Env& e, int l) {
+    const LvlView L = view(const_cast<Env&>(e), l);
+    if (L.X % 4 != 0) return false;
+    if (l > 0) return (L.Y % 2 == 0) && (L.Z % 2 == 0);
+    const int gx = (L.X / 4 + 31) / 32, gy = (L.Y + JVY - 1) / JVY;
+    return gx * gy <= kMaxPartials && (L.Y % 2 == 0) && (L.Z % 2 == 0);
+}
+
+template <class CT>
+void vcycle_vec(Env& e, int l, const CT* ax, const CT* ay, const CT* az, const CT* aw, const float* b, float* x, float* x2,
+                const int* skip, int dot);
+
+// z = V(b) on level l (level 0: x = z0, x2 = z0b). skip: the kernels return at once while *skip
+// is set (the CG has converged inside a chunk of queued iterations). On a vector finest level
+// dot = DOT_START / DOT_NEXT also forms z.r in the last smoothing step (returns true).
+bool vcycle(Env& e, int l, const float* b, float* x, float* x2, const int* skip, int dot) {
     const LvlView L = view(e, l);
     if (l == e.mg_levels) {
         const int n = L.X * L.Y * L.Z;
-        k_mg_coarse<<<1, 512, 2 * n * sizeof(float), e.stream>>>(L, b, x);
+        k_mg_coarse<<<1, 512, 2 * n * sizeof(float), e.stream>>>(L, b, x, skip);
         e.launches += 1;
-        return;
+        return false;
+    }
+    if (vec_level(e, l)) {
+        if (l == 0 && e.cfg.mg_half) {
+            __half* h[4];
+            half_arrays(e, h);
+            vcycle_vec<__half>(e, 0, h[0], h[1], h[2], h[3], b, x, x2, skip, dot);
+        } else {
+            vcycle_vec<float>(e, l, L.ax, L.ay, L.az, L.aw, b, x, x2, skip, dot);
+        }
+        return l == 0 && dot != DOT_NONE;
     }
     const dim3 gr = lgrid(L.X, L.Y, L.Z), bl(MBX, MBY);
     MgLevel& C = e.mg[l + 1];
     const float c2a = 1.0f / kChebTheta;
-    if (l == 0 && (e.g.X % 4) == 0) {
-        const Grid& g = e.g;
-        const int n4 = g.N / 4;
-        const int ns = std::min((n4 + RT - 1) / RT, e.num_sms * 8);
-        const int gx = (g.X / 4 + 31) / 32, gy = (g.Y + JVY - 1) / JVY;
-        int zc = std::max(1, std::min(g.Z, (e.num_sms * 12 + gx * gy - 1) / (gx * gy)));
-        const int zlen = (g.Z + zc - 1) / zc;
-        zc = (g.Z + zlen - 1) / zlen;
-        const dim3 jg(gx, gy, zc), jb(32, JVY);
-        // pre-smoothing from zero: A -> x2, B -> x
-        k_mg_first4<<<ns, RT, 0, e.stream>>>(n4, (const float4*)e.aw, (const float4*)b, (float4*)x2);
-        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, nullptr, x, b, kChebC1, kChebC2);
-        k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b);
-        vcycle(e, l + 1, C.b, C.x, C.x2);
-        k_mg_prolong4<<<ns, RT, 0, e.stream>>>(g, C.X, C.Y, C.x, e.aw, x);
-        // post-smoothing: A x -> x2, B (x2, prev x) -> x
-        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x, nullptr, x2, b, 0.0f, c2a);
-        k_mg_jacobi4<<<jg, jb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, x2, x, x, b, kChebC1, kChebC2);
-        e.launches += 6;
-        return;
-    }
-    k_mg_jacobi<true><<<gr, bl, 0, e.stream>>>(L, nullptr, nullptr, x2, b, 0.0f, 0.0f);
-    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, nullptr, x, b, kChebC1, kChebC2);
-    k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b);
-    vcycle(e, l + 1, C.b, C.x, C.x2);
-    k_mg_prolong<<<gr, bl, 0, e.stream>>>(L, x, C.X, C.Y, C.x);
-    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x, nullptr, x2, b, 0.0f, c2a);
-    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, x, b, kChebC1, kChebC2);
+    k_mg_jacobi<true><<<gr, bl, 0, e.stream>>>(L, nullptr, nullptr, x2, b, 0.0f, 0.0f, skip);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, nullptr, x, b, kChebC1, kChebC2, skip);
+    k_mg_restrict<<<lgrid(C.X, C.Y, C.Z), bl, 0, e.stream>>>(L, x, b, C.X, C.Y, C.Z, C.b, skip);
+    vcycle(e, l + 1, C.b, C.x, C.x2, skip, DOT_NONE);
+    k_mg_prolong<<<gr, bl, 0, e.stream>>>(L, x, C.X, C.Y, C.x, skip);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x, nullptr, x2, b, 0.0f, c2a, skip);
+    k_mg_jacobi<false><<<gr, bl, 0, e.stream>>>(L, x2, x, x, b, kChebC1, kChebC2, skip);
     e.launches += 6;
+    return false;
+}
+
+template <class CT>
+void vcycle_vec(Env& e, int l, const CT* ax, const CT* ay, const CT* az, const CT* aw, const float* b, float* x, float* x2,
+                const int* skip, int dot) {
+    const LvlView L = view(e, l);
+    MgLevel& C = e.mg[l + 1];
+    const March m = march(e, L.X, L.Y, L.Z);
+    const dim3 jb(32, JVY);
+    const float c2a = 1.0f / kChebTheta;
+    UIn<SM_PRE, CT> upre{b, aw, nullptr, 0, 0};
+    UIn<SM_POSTA, CT> upost{x, aw, C.x, C.X, C.Y};
+    UIn<SM_POSTB, CT> ub{x2, aw, nullptr, 0, 0};
+    // pre-smoothing from zero (steps A and B in one pass) -> x
+    k_mg_smooth4<SM_PRE, DOT_NONE, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, upre, upost, x,
+                                                                   kChebC1, kChebC2, skip, e.sc, e.partials);
+    k_mg_restrict4<CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, x, b, C.X, C.Y, C.b, skip);
+    vcycle(e, l + 1, C.b, C.x, C.x2, skip, DOT_NONE);
+    // post-smoothing: step A on x + P e -> x2, step B (prev = x + P e) -> x
+    k_mg_smooth4<SM_POSTA, DOT_NONE, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, upost, upost, x2,
+                                                                     0.0f, c2a, skip, e.sc, e.partials);
+    if (dot == DOT_START)
+        k_mg_smooth4<SM_POSTB, DOT_START, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, ub, upost, x,
+                                                                          kChebC1, kChebC2, skip, e.sc, e.partials);
+    else if (dot == DOT_NEXT)
+        k_mg_smooth4<SM_POSTB, DOT_NEXT, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, ub, upost, x,
+                                                                         kChebC1, kChebC2, skip, e.sc, e.partials);
+    else
+        k_mg_smooth4<SM_POSTB, DOT_NONE, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, ub, upost, x,
+                                                                         kChebC1, kChebC2, skip, e.sc, e.partials);
+    e.launches += 4;
 }
 
 }  // namespace
@@ -649,6 +990,7 @@ void mg_solve(Env& e) {
         cudaMemsetAsync(&e.sc->outer_inner_total, 0, sizeof(int), e.stream);
         e.launches += 1;
     }
+    const bool fused = e.mg_levels > 0 && vec_level(e, 0);
     int outer = 0;
     const int max_outer = 12;
     for (; outer < max_outer; ++outer) {
@@ -661,9 +1003,40 @@ void mg_solve(Env& e) {
         cudaStreamSynchronize(e.stream);
         if (e.host_sc->refine_done == 1) break;
         // inner MG-PCG on A e = r
+        const int* conv = &e.sc->converged;
+        if (fused) {
+            // the V-cycle's last smoothing step forms z.r; the operator kernel forms the search
+            // direction, written to the other buffer of the (s, pp) pair each iteration
+            float* s_old = e.s;
+            float* s_new = e.pp;
+            { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, nullptr, DOT_START); }
+            const March m = march(e, g.X, g.Y, g.Z);
+            const int chunk = 4;
+            for (int it = 0; it < e.cfg.inner_max_iter; it += chunk) {
+                for (int k = 0; k < chunk && it + k < e.cfg.inner_max_iter; ++k) {
+                    { ProfScope ps(e, "mg_matvec");
+                      k_mg_matvec_search4<<<m.grid, dim3(32, JVY), 0, e.stream>>>(g.X, g.Y, g.Z, m.zlen, e.ax, e.ay, e.az, e.aw, z0, s_old,
+                                                                                s_new, e.As, e.sc, e.partials);
+                      e.launches += 1; }
+                    { ProfScope ps(e, "mg_update");
+                      k_update_mg4<<<nb, RT, 0, e.stream>>>(n / 4, (const float4*)s_new, (const float4*)e.As, (float4*)ecor, (float4*)e.r,
+                                                           e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials);
+                      e.launches += 1; }
+                    { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NEXT); }
+                    std::swap(s_old, s_new);
+                }
+                cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
+                cudaStreamSynchronize(e.stream);
+                if (e.host_sc->converged) break;
+            }
+            { ProfScope ps(e, "mg_refine");
+              k_accum64<<<nb, RT, 0, e.stream>>>(n, e.xd, ecor);
+              e.launches += 1; }
+            continue;
+        }
         {
             ProfScope ps(e, "mg_vcycle");
-            vcycle(e, 0, e.r, z0, z0b);
+            vcycle(e, 0, e.r, z0, z0b, nullptr, DOT_NONE);
         }
         const bool vec = (g.X % 4) == 0;
         const int n4 = n / 4;
@@ -678,7 +1051,7 @@ void mg_solve(Env& e) {
                     { ProfScope ps(e, "mg_update");
                       k_update_mg4<<<nb, RT, 0, e.stream>>>(n4, (const float4*)e.s, (const float4*)e.As, (float4*)ecor, (float4*)e.r,
                                                            e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials); }
-                    { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b); }
+                    { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NONE); }
                     { ProfScope ps(e, "mg_search");
                       k_zr4<false><<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (const float4*)e.r, nullptr, e.sc, e.partials);
                       k_search_mg4<<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (float4*)e.s, e.sc); }
@@ -689,7 +1062,7 @@ void mg_solve(Env& e) {
                   k_matvec_mg<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, e.s, e.As, e.sc, e.partials); }
                 { ProfScope ps(e, "mg_update");
                   k_update_mg<<<nb, RT, 0, e.stream>>>(n, e.s, e.As, ecor, e.r, e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials); }
-                { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b); }
+                { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NONE); }
                 { ProfScope ps(e, "mg_search");
                   k_zr_search<false><<<nb, RT, 0, e.stream>>>(n, z0, e.r, e.s, e.sc, e.partials);
                   k_search_mg<<<nb, RT, 0, e.stream>>>(n, z0, e.s, e.sc); }

@@ -102,10 +102,12 @@ class SolverConfig:
     inner_max_iter: int = 60
     inner_rtol: float = 1e-4
     use_graph: int = 0
+    mg_half: int = 1            # mixed: FP16 finest-level coefficients inside the V-cycle
 
     def c(self):
         return _lib.SolverCfg(self.semantics, self.diffuse_sweeps, self.pcg_tol, self.pcg_max_iter, self.max_substeps,
-                              self.precision, self.refine_tol, self.inner_max_iter, self.inner_rtol, self.use_graph)
+                              self.precision, self.refine_tol, self.inner_max_iter, self.inner_rtol, self.use_graph,
+                              self.mg_half)
 
 
 def _fp(a):

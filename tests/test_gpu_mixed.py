@@ -44,17 +44,20 @@ FP64_CFG = dict(semantics=1, pcg_tol=1e-13, pcg_max_iter=20000)
 
 @pytest.fixture(scope="module")
 def developed():
-    init, dt, speed = small_case(SHAPE)
+    return _developed(SHAPE)
+
+
+def _developed(shape):
+    init, dt, speed = small_case(shape)
     st = oracle.OracleState(init, np.float32)
     for _ in range(2):
         st.step(oracle.Config(semantics=1), dt, speed)
     return init, dt, speed, st
 
 
-def test_mixed_projection_matches_fp64(gpu_lib, developed):
-    init, dt, speed, st32 = developed
+def _check_projection(init, dt, speed, st32, cfg, max_inner=None):
     ref = _to64(st32, init)
-    env = make_env(init, SolverConfig(precision=1, refine_tol=1e-8))
+    env = make_env(init, cfg)
     push_oracle_to_env(st32, env)
     g = env.run_stage(3, 0, dt * speed)
     o = ref.stage(oracle.Config(**FP64_CFG), 3, 0, dt * speed)
@@ -62,11 +65,28 @@ def test_mixed_projection_matches_fp64(gpu_lib, developed):
     st = env.stats()
     assert st["converged"] and st["pcg_residual"] <= 1e-8, st
     assert st["outer_iters"] >= 1
+    if max_inner is not None:
+        assert st["pcg_iters"] <= max_inner, st
     m = ref.sky_mask()
     for k in ("u", "v", "w", "p", "rho"):
         e = rel_l2(env.read(k), ref.a[k], m)
         assert e <= 1e-6, (k, e, g, st)
     env.close()
+
+
+@pytest.mark.parametrize("mg_half", [1, 0])
+def test_mixed_projection_matches_fp64(gpu_lib, developed, mg_half):
+    """32^3: the fused float4 V-cycle on the finest level, FP16 or FP32 smoother coefficients."""
+    init, dt, speed, st32 = developed
+    _check_projection(init, dt, speed, st32, SolverConfig(precision=1, refine_tol=1e-8, mg_half=mg_half))
+
+
+@pytest.mark.parametrize("shape,max_inner", [((64, 64, 32), 40), ((30, 20, 20), 60), ((36, 28, 24), 60)])
+def test_mixed_projection_hierarchies(gpu_lib, shape, max_inner):
+    """64x64x32 runs two vector coarse levels; x = 30 runs the scalar finest level with the
+    unfused CG; 36x28x24 a vector finest level over a coarsest level of odd x size."""
+    init, dt, speed, st32 = _developed(shape)
+    _check_projection(init, dt, speed, st32, SolverConfig(precision=1, refine_tol=1e-8), max_inner)
 
 
 def test_mixed_steps_match_fp64(gpu_lib):
