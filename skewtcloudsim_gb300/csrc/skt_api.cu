@@ -334,7 +334,14 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     cudaEventSynchronize(e.ev1);
     cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
     const skt_status st = cuda_check(e, "step");
-    return st != SKT_OK ? st : worst;
+    if (st != SKT_OK) return st;
+    int dev_status = 0;
+    cudaMemcpy(&dev_status, &e.sc->status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (dev_status != 0) {
+        cudaMemset(&e.sc->status, 0, sizeof(int));
+        return fail(&e, skt_status(dev_status), "a kernel gave up waiting for its streamed data (device-side wait limit)");
+    }
+    return worst;
 }
 
 skt_status skt_sync(skt_env* env) {

@@ -125,9 +125,11 @@ __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const f
     }
 }
 
-// advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp)
-__device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float vR, float dt, float vox) {
-    float C = veli * dt / vox;
+// advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp).
+// cdt = dt/vox: the Courant number is veli*cdt (the reference divides veli*dt by vox each call)
+// and the limiter ratios use the fast divide; both change results by a few ulp at most.
+__device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float vR, float cdt) {
+    float C = veli * cdt;
     C = C > 1.0f ? 1.0f : (C < -1.0f ? -1.0f : C);
     const float qMin = fminf(vL, fminf(vC, vR));
     const float qMax = fmaxf(vL, fmaxf(vC, vR));
@@ -140,8 +142,8 @@ __device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float 
     }
     const float qLS = vC - 0.5f * s, qRS = vC + 0.5f * s;
     float B = 1.0f;
-    if (qRS > qMax) { const float den = qRS - vC; if (den > 1e-16f) B = fminf(B, (qMax - vC) / den); }
-    if (qLS < qMin) { const float den = vC - qLS; if (den > 1e-16f) B = fminf(B, (vC - qMin) / den); }
+    if (qRS > qMax) { const float den = qRS - vC; if (den > 1e-16f) B = fminf(B, __fdividef(qMax - vC, den)); }
+    if (qLS < qMin) { const float den = vC - qLS; if (den > 1e-16f) B = fminf(B, __fdividef(vC - qMin, den)); }
     float qR = vC + B * (qRS - vC);
     float qL = vC + B * (qLS - vC);
     if ((qR - vC) * (vC - qL) <= 0.0f) { qR = qL = vC; }
@@ -149,6 +151,22 @@ __device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float 
     if (C > 0.0f) qq = qR + C * (-qL - 2 * qR + 3 * vC) + C * C * (qL + qR - 2 * vC);
     else qq = qR + C * (-2 * qL - qR + 3 * vC) + C * C * (qL + qR - 2 * vC);
     return veli * qq;
+}
+
+// The flux through the face between cells b (below) and c (above) with face velocity u, a below b
+// and d above c: the reconstruction is taken on the upwind side (a, b, c for u >= 0, else d, c, b).
+// A cell's upper-face flux (its velocity, window q-1..q+2) and the next cell's lower-face flux
+// (the previous cell's velocity, window q-2..q+1 seen from it) are the same call, so each face is
+// computed once and handed on. For a window of ones the flux is exactly u.
+__device__ __forceinline__ float face_flux(float u, float a, float b, float c, float d, float cdt) {
+    return u >= 0.0f ? ppm_flux(u, a, b, c, cdt) : ppm_flux(u, d, c, b, cdt);
+}
+
+// the advected value over the advected density companion (divideValues Game/kernelMaths.cu:38)
+__device__ __forceinline__ float ppm_update(float q, float fp, float fm, float fpo, float fmo, float cdt) {
+    const float nq = q - cdt * (fp - fm);
+    const float nr = 1.0f - cdt * (fpo - fmo);
+    return nq / nr;
 }
 
 // ghost value of the density companion (a field of ones, custom value 1)
@@ -176,12 +194,12 @@ __global__ void __launch_bounds__(256) k_ppm(Grid g, const float* __restrict__ i
     }
     const float dtSub = dtFull / float(nsub);
     const float dt = half ? dtSub * 0.5f : dtSub;
+    const float cdt = dt / g.vox;
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
     if (x >= g.X || y >= g.Y) return;
     if (is_ground(g, x, y, z)) return;
     constexpr int ax = AXIS == 0, ay = AXIS == 1, az = AXIS == 2;
     const int c = cidx(g, x, y, z);
-    const float vox = g.vox;
     float q[5], o[5];
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
@@ -193,72 +211,35 @@ __global__ void __launch_bounds__(256) k_ppm(Grid g, const float* __restrict__ i
     const float custom = AXIS == 0 ? defU[y] : (AXIS == 1 ? 0.0f : defW[y]);
     const float vc = vel[c];
     const float vm = face_nb(g, vel, x, y, z, -ax, -ay, -az, sides, ground, custom);
-    float nq, nr;
-    {
-        float L, C, R;
-        if (vc >= 0.0f) { L = q[1]; C = q[2]; R = q[3]; } else { L = q[4]; C = q[3]; R = q[2]; }
-        const float fp = ppm_flux(vc, L, C, R, dt, vox);
-        if (vm < 0.0f) { L = q[3]; C = q[2]; R = q[1]; } else { L = q[0]; C = q[1]; R = q[2]; }
-        const float fm = ppm_flux(vm, L, C, R, dt, vox);
-        nq = in[c] - (dt / vox) * (fp - fm);
-    }
-    {
-        float L, C, R;
-        if (vc >= 0.0f) { L = o[1]; C = o[2]; R = o[3]; } else { L = o[4]; C = o[3]; R = o[2]; }
-        const float fp = ppm_flux(vc, L, C, R, dt, vox);
-        if (vm < 0.0f) { L = o[3]; C = o[2]; R = o[1]; } else { L = o[0]; C = o[1]; R = o[2]; }
-        const float fm = ppm_flux(vm, L, C, R, dt, vox);
-        nr = 1.0f - (dt / vox) * (fp - fm);
-    }
-    out[c] = nq / nr;
-}
-
-// One cell of a directional PPM pass from its 5-value windows (q and the density companion):
-// the same arithmetic as k_ppm.
-// When the companion's window is all ones its reconstruction is exactly 1 (the slope, limiter and
-// parabola terms all vanish), so its face fluxes are exactly the face velocities; the two
-// ppm_flux calls are skipped with a bit-identical result.
-__device__ __forceinline__ float ppm_cell(const float* q, const float* o, float vc, float vm, float dt, float vox) {
-    float nq, nr;
-    const bool ones = o[0] == 1.0f && o[1] == 1.0f && o[3] == 1.0f && o[4] == 1.0f;
-    {
-        float L, C, R;
-        if (vc >= 0.0f) { L = q[1]; C = q[2]; R = q[3]; } else { L = q[4]; C = q[3]; R = q[2]; }
-        const float fp = ppm_flux(vc, L, C, R, dt, vox);
-        if (vm < 0.0f) { L = q[3]; C = q[2]; R = q[1]; } else { L = q[0]; C = q[1]; R = q[2]; }
-        const float fm = ppm_flux(vm, L, C, R, dt, vox);
-        nq = q[2] - (dt / vox) * (fp - fm);
-    }
-    if (ones) {
-        nr = 1.0f - (dt / vox) * (vc - vm);
-    } else {
-        float L, C, R;
-        if (vc >= 0.0f) { L = o[1]; C = o[2]; R = o[3]; } else { L = o[4]; C = o[3]; R = o[2]; }
-        const float fp = ppm_flux(vc, L, C, R, dt, vox);
-        if (vm < 0.0f) { L = o[3]; C = o[2]; R = o[1]; } else { L = o[0]; C = o[1]; R = o[2]; }
-        const float fm = ppm_flux(vm, L, C, R, dt, vox);
-        nr = 1.0f - (dt / vox) * (fp - fm);
-    }
-    return nq / nr;
+    const float fp = face_flux(vc, q[1], q[2], q[3], q[4], cdt), fm = face_flux(vm, q[0], q[1], q[2], q[3], cdt);
+    const float fpo = face_flux(vc, o[1], o[2], o[3], o[4], cdt), fmo = face_flux(vm, o[0], o[1], o[2], o[3], cdt);
+    out[c] = ppm_update(q[2], fp, fm, fpo, fmo, cdt);
 }
 
 __device__ __forceinline__ float comp(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+__device__ __forceinline__ void setc(float4& v, int k, float a) {
+    if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
+}
 
-// Vectorised PPM pass for flat terrain and X % 4 == 0 (four cells per thread along x; the Z pass
-// marches with a five-plane window in registers).
-template <int AXIS>
-__global__ void __launch_bounds__(32 * DVY) k_ppm4(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
-                                                   const float* __restrict__ vel, const float* __restrict__ def, int sides, int ground,
-                                                   const float* __restrict__ defU, const float* __restrict__ defW, float dtFull,
-                                                   int nsub_host, int half, const Scalars* __restrict__ sc, int slot) {
+__device__ __forceinline__ float ppm_cdt(const Grid& g, float dtFull, int nsub, int half) {
+    const float dtSub = dtFull / float(nsub);
+    const float dt = half ? dtSub * 0.5f : dtSub;
+    return dt / g.vox;
+}
+
+// Vectorised X pass (flat terrain, X % 4 == 0): a thread owns four cells of one row and marches
+// z. Its four upper-face fluxes use the x window q(x0-2) .. q(x0+5); the lower face of its first
+// cell is the upper face of the lane before it (a shuffle), computed directly by lane 0.
+__global__ void __launch_bounds__(32 * DVY) k_ppm4x(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
+                                                    const float* __restrict__ vel, const float* __restrict__ def, int sides,
+                                                    const float* __restrict__ defU, float dtFull, int nsub_host, int half,
+                                                    const Scalars* __restrict__ sc, int slot) {
     int nsub = nsub_host;
     if (sc) {
         nsub = sc->nsub;
         if (slot >= nsub) return;
     }
-    const float dtSub = dtFull / float(nsub);
-    const float dt = half ? dtSub * 0.5f : dtSub;
-    const float vox = g.vox;
+    const float cdt = ppm_cdt(g, dtFull, nsub, half);
     const int lane = threadIdx.x;
     const int x0 = (blockIdx.x * 32 + lane) * 4;
     const int y = blockIdx.y * DVY + threadIdx.y + 1;
@@ -267,104 +248,179 @@ __global__ void __launch_bounds__(32 * DVY) k_ppm4(Grid g, int zlen, const float
     const int X = g.X, XY = g.XY;
     const int row = x0 + y * X;
     const float dy = act ? (def ? def[y] : 0.0f) : 0.0f;
-    const float dyt = def ? def[g.Y - 1] : 0.0f;
-    const float dg0 = def ? def[0] : 0.0f;
-    const float gq = bc_val(ground, 0.0f, dg0);   // ground ghost of q (ground is never NEUMANN here)
-    const float go = bc_val(ground, 1.0f, 1.0f);  // ground ghost of the density companion
-    const float so = bc_val(sides, 1.0f, 1.0f);   // side ghost of the density companion
-    if (AXIS == 2) {
-        // window planes z-2 .. z+2
-        float4 w0 = make_float4(0, 0, 0, 0), w1 = w0, w2 = w0, w3 = w0, w4 = w0, vb = w0;
-        auto side4 = [&](const float4& b) {
-            return make_float4(bc_val(sides, b.x, dy), bc_val(sides, b.y, dy), bc_val(sides, b.z, dy), bc_val(sides, b.w, dy));
-        };
-        if (act) {
-            w2 = ld4f(in, row + zs * XY);
-            w1 = zs >= 1 ? ld4f(in, row + (zs - 1) * XY) : side4(w2);
-            w0 = zs >= 2 ? ld4f(in, row + (zs - 2) * XY) : (zs == 1 ? side4(w1) : side4(w2));
-            w3 = zs + 1 < g.Z ? ld4f(in, row + (zs + 1) * XY) : side4(w2);
-            if (zs > 0) vb = ld4f(vel, row + (zs - 1) * XY);
-        }
-        for (int z = zs; z < ze; ++z) {
-            const int c = row + z * XY;
-            if (act) {
-                if (z + 2 < g.Z) w4 = ld4f(in, c + 2 * XY);
-                else w4 = z + 1 < g.Z ? side4(w3) : side4(w2);
-                const float4 vc4 = ld4f(vel, c);
-                float4 vm4 = vb;
-                if (z == 0) {
-                    const float cu = defW[y];
-                    vm4 = make_float4(bc_val(sides, vc4.x, cu), bc_val(sides, vc4.y, cu), bc_val(sides, vc4.z, cu), bc_val(sides, vc4.w, cu));
-                }
-                float4 o4;
+    const float du = act ? defU[y] : 0.0f;
+    const float so = bc_val(sides, 1.0f, 1.0f);
+    const bool xedge = x0 < 4 || x0 + 8 > X;  // the companion window reaches outside the domain
+    float ow[8];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const float q[5] = {comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k)};
-                    const float o[5] = {z >= 2 ? 1.0f : so, z >= 1 ? 1.0f : so, 1.0f, z + 1 < g.Z ? 1.0f : so, z + 2 < g.Z ? 1.0f : so};
-                    const float r = ppm_cell(q, o, comp(vc4, k), comp(vm4, k), dt, vox);
-                    if (k == 0) o4.x = r; else if (k == 1) o4.y = r; else if (k == 2) o4.z = r; else o4.w = r;
-                }
-                *reinterpret_cast<float4*>(out + c) = o4;
-                vb = vc4;
-            }
-            w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+    for (int j = 0; j < 8; ++j) ow[j] = (x0 - 2 + j >= 0 && x0 - 2 + j < X) ? 1.0f : so;
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 qc = make_float4(0, 0, 0, 0), uc = qc;
+        if (act) { qc = ld4f(in, c); uc = ld4f(vel, c); }
+        float qm2 = __shfl_up_sync(0xffffffffu, qc.z, 1), qm1 = __shfl_up_sync(0xffffffffu, qc.w, 1);
+        float qp4 = __shfl_down_sync(0xffffffffu, qc.x, 1), qp5 = __shfl_down_sync(0xffffffffu, qc.y, 1);
+        float um1 = __shfl_up_sync(0xffffffffu, uc.w, 1);
+        if (act && lane == 0) {
+            if (x0 >= 4) { qm2 = in[c - 2]; qm1 = in[c - 1]; um1 = vel[c - 1]; }
+            else { qm2 = qm1 = bc_val(sides, qc.x, dy); um1 = bc_val(sides, uc.x, du); }
         }
-        return;
+        if (act && (lane == 31 || x0 + 4 >= X)) {
+            if (x0 + 4 < X) { qp4 = in[c + 4]; qp5 = in[c + 5]; }
+            else { qp4 = qp5 = bc_val(sides, qc.w, dy); }
+        }
+        const float w[8] = {qm2, qm1, qc.x, qc.y, qc.z, qc.w, qp4, qp5};
+        const float u[4] = {uc.x, uc.y, uc.z, uc.w};
+        float F[4], Fo[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            F[k] = face_flux(u[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], cdt);
+            Fo[k] = xedge ? face_flux(u[k], ow[k + 1], ow[k + 2], ow[k + 3], ow[k + 4], cdt) : u[k];
+        }
+        float Fm = __shfl_up_sync(0xffffffffu, F[3], 1);
+        float Fmo = __shfl_up_sync(0xffffffffu, Fo[3], 1);
+        if (lane == 0) {
+            Fm = face_flux(um1, w[0], w[1], w[2], w[3], cdt);
+            Fmo = xedge ? face_flux(um1, ow[0], ow[1], ow[2], ow[3], cdt) : um1;
+        }
+        if (act) {
+            float4 o4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float fm = k == 0 ? Fm : F[k - 1], fmo = k == 0 ? Fmo : Fo[k - 1];
+                setc(o4, k, ppm_update(w[k + 2], F[k], fm, Fo[k], fmo, cdt));
+            }
+            *reinterpret_cast<float4*>(out + c) = o4;
+        }
+    }
+}
+
+// Vectorised Y pass: a thread owns four cells of one (x, z) column and marches a run of rows,
+// keeping the window q(y-2) .. q(y+2) in registers and handing each upper-face flux on as the next
+// row's lower-face flux. Rows <= 0 are the ground ghost, rows >= Y the side ghost of the top row.
+constexpr int PY = 4;
+__global__ void __launch_bounds__(32 * PY) k_ppm4y(Grid g, int ylen, const float* __restrict__ in, float* __restrict__ out,
+                                                   const float* __restrict__ vel, const float* __restrict__ def, int sides, int ground,
+                                                   float dtFull, int nsub_host, int half, const Scalars* __restrict__ sc, int slot) {
+    int nsub = nsub_host;
+    if (sc) {
+        nsub = sc->nsub;
+        if (slot >= nsub) return;
+    }
+    const float cdt = ppm_cdt(g, dtFull, nsub, half);
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int z = blockIdx.y * PY + threadIdx.y;
+    const int ys = 1 + blockIdx.z * ylen, ye = min(ys + ylen, g.Y);
+    if (x0 >= g.X || z >= g.Z || ys >= g.Y) return;
+    const int X = g.X, Y = g.Y;
+    const int base = x0 + z * g.XY;
+    const float dyt = def ? def[Y - 1] : 0.0f;
+    const float gq = bc_val(ground, 0.0f, def ? def[0] : 0.0f);
+    const float go = bc_val(ground, 1.0f, 1.0f), so = bc_val(sides, 1.0f, 1.0f);
+    auto qrow = [&](int r) -> float4 {
+        if (r <= 0) return make_float4(gq, gq, gq, gq);
+        if (r < Y) return ld4f(in, base + r * X);
+        const float4 t = ld4f(in, base + (Y - 1) * X);
+        return make_float4(bc_val(sides, t.x, dyt), bc_val(sides, t.y, dyt), bc_val(sides, t.z, dyt), bc_val(sides, t.w, dyt));
+    };
+    auto orow = [&](int r) { return r <= 0 ? go : (r < Y ? 1.0f : so); };
+    float4 w0 = qrow(ys - 2), w1 = qrow(ys - 1), w2 = qrow(ys), w3 = qrow(ys + 1);
+    float4 Fc, Fco;  // lower-face fluxes of the current row
+    {
+        const float4 vm = ys >= 2 ? ld4f(vel, base + (ys - 1) * X) : make_float4(0, 0, 0, 0);  // face below y = 1 is ground: 0
+        const bool oin = ys >= 3 && ys + 1 < Y;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float u = comp(vm, k);
+            setc(Fc, k, face_flux(u, comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), cdt));
+            setc(Fco, k, oin ? u : face_flux(u, orow(ys - 2), orow(ys - 1), orow(ys), orow(ys + 1), cdt));
+        }
+    }
+    for (int y = ys; y < ye; ++y) {
+        const float4 w4 = qrow(y + 2);
+        const float4 vc = ld4f(vel, base + y * X);
+        const bool oin = y >= 2 && y + 2 < Y;
+        float4 Fp, Fpo, o4;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float u = comp(vc, k);
+            setc(Fp, k, face_flux(u, comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k), cdt));
+            setc(Fpo, k, oin ? u : face_flux(u, orow(y - 1), orow(y), orow(y + 1), orow(y + 2), cdt));
+            setc(o4, k, ppm_update(comp(w2, k), comp(Fp, k), comp(Fc, k), comp(Fpo, k), comp(Fco, k), cdt));
+        }
+        *reinterpret_cast<float4*>(out + base + y * X) = o4;
+        Fc = Fp;
+        Fco = Fpo;
+        w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+    }
+}
+
+// Vectorised Z pass: the z march keeps the window q(z-2) .. q(z+2) and hands each upper-face
+// flux on as the next plane's lower-face flux (computed directly at the first plane of a run; at
+// z = 0 the face velocity is the boundary value).
+__global__ void __launch_bounds__(32 * DVY) k_ppm4z(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
+                                                    const float* __restrict__ vel, const float* __restrict__ def, int sides,
+                                                    const float* __restrict__ defW, float dtFull, int nsub_host, int half,
+                                                    const Scalars* __restrict__ sc, int slot) {
+    int nsub = nsub_host;
+    if (sc) {
+        nsub = sc->nsub;
+        if (slot >= nsub) return;
+    }
+    const float cdt = ppm_cdt(g, dtFull, nsub, half);
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * DVY + threadIdx.y + 1;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    if (x0 >= g.X || y >= g.Y) return;
+    const int X = g.X, XY = g.XY, Z = g.Z;
+    const int row = x0 + y * X;
+    const float dy = def ? def[y] : 0.0f;
+    const float so = bc_val(sides, 1.0f, 1.0f);
+    auto side4 = [&](const float4& b) {
+        return make_float4(bc_val(sides, b.x, dy), bc_val(sides, b.y, dy), bc_val(sides, b.z, dy), bc_val(sides, b.w, dy));
+    };
+    auto oz = [&](int zz) { return (zz >= 0 && zz < Z) ? 1.0f : so; };
+    float4 w2 = ld4f(in, row + zs * XY);
+    float4 w1 = zs >= 1 ? ld4f(in, row + (zs - 1) * XY) : side4(w2);
+    float4 w0 = zs >= 2 ? ld4f(in, row + (zs - 2) * XY) : (zs == 1 ? side4(w1) : side4(w2));
+    float4 w3 = zs + 1 < Z ? ld4f(in, row + (zs + 1) * XY) : side4(w2);
+    float4 Fc, Fco;
+    {
+        float4 vm;
+        if (zs == 0) {
+            const float4 v0 = ld4f(vel, row);
+            const float cu = defW[y];
+            vm = make_float4(bc_val(sides, v0.x, cu), bc_val(sides, v0.y, cu), bc_val(sides, v0.z, cu), bc_val(sides, v0.w, cu));
+        } else {
+            vm = ld4f(vel, row + (zs - 1) * XY);
+        }
+        const bool oin = zs >= 2 && zs + 1 < Z;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float u = comp(vm, k);
+            setc(Fc, k, face_flux(u, comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), cdt));
+            setc(Fco, k, oin ? u : face_flux(u, oz(zs - 2), oz(zs - 1), oz(zs), oz(zs + 1), cdt));
+        }
     }
     for (int z = zs; z < ze; ++z) {
         const int c = row + z * XY;
-        if (AXIS == 0) {
-            float4 qc = make_float4(0, 0, 0, 0), uc = qc;
-            if (act) { qc = ld4f(in, c); uc = ld4f(vel, c); }
-            float qm2 = __shfl_up_sync(0xffffffffu, qc.z, 1), qm1 = __shfl_up_sync(0xffffffffu, qc.w, 1);
-            float qp4 = __shfl_down_sync(0xffffffffu, qc.x, 1), qp5 = __shfl_down_sync(0xffffffffu, qc.y, 1);
-            float um1 = __shfl_up_sync(0xffffffffu, uc.w, 1);
-            if (!act) continue;
-            if (lane == 0) {
-                if (x0 >= 2) { qm2 = in[c - 2]; qm1 = in[c - 1]; um1 = vel[c - 1]; }
-                else { qm2 = qm1 = bc_val(sides, qc.x, dy); um1 = bc_val(sides, uc.x, defU[y]); }
-            }
-            if (lane == 31 || x0 + 4 >= X) {
-                if (x0 + 4 < X) { qp4 = in[c + 4]; qp5 = in[c + 5]; }
-                else { qp4 = qp5 = bc_val(sides, qc.w, dy); }
-            }
-            const float w[8] = {qm2, qm1, qc.x, qc.y, qc.z, qc.w, qp4, qp5};
-            const float vcs[4] = {uc.x, uc.y, uc.z, uc.w};
-            const float vms[4] = {um1, uc.x, uc.y, uc.z};
-            float4 o4;
+        const float4 w4 = z + 2 < Z ? ld4f(in, c + 2 * XY) : (z + 1 < Z ? side4(w3) : side4(w2));
+        const float4 vc = ld4f(vel, c);
+        const bool oin = z >= 1 && z + 2 < Z;
+        float4 Fp, Fpo, o4;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int x = x0 + k;
-                const float o[5] = {x >= 2 ? 1.0f : so, x >= 1 ? 1.0f : so, 1.0f, x + 1 < X ? 1.0f : so, x + 2 < X ? 1.0f : so};
-                const float r = ppm_cell(&w[k], o, vcs[k], vms[k], dt, vox);
-                if (k == 0) o4.x = r; else if (k == 1) o4.y = r; else if (k == 2) o4.z = r; else o4.w = r;
-            }
-            *reinterpret_cast<float4*>(out + c) = o4;
-        } else {
-            if (!act) continue;
-            const float4 qc = ld4f(in, c), vc4 = ld4f(vel, c);
-            const float4 gq4 = make_float4(gq, gq, gq, gq);
-            const float4 qd1 = y >= 2 ? ld4f(in, c - X) : gq4;
-            const float4 qd2 = y >= 3 ? ld4f(in, c - 2 * X) : gq4;
-            float4 qu1, qu2;
-            if (y + 1 < g.Y) qu1 = ld4f(in, c + X);
-            else qu1 = make_float4(bc_val(sides, qc.x, dy), bc_val(sides, qc.y, dy), bc_val(sides, qc.z, dy), bc_val(sides, qc.w, dy));
-            if (y + 2 < g.Y) qu2 = ld4f(in, c + 2 * X);
-            else if (y + 1 < g.Y) {
-                const float4 b = qu1;  // the clamped cell is the top row y+1 = Y-1
-                qu2 = make_float4(bc_val(sides, b.x, dyt), bc_val(sides, b.y, dyt), bc_val(sides, b.z, dyt), bc_val(sides, b.w, dyt));
-            } else qu2 = qu1;
-            const float4 vm4 = y >= 2 ? ld4f(vel, c - X) : make_float4(0, 0, 0, 0);  // face below y = 1 is ground: 0
-            const float o2[5] = {y >= 3 ? 1.0f : go, y >= 2 ? 1.0f : go, 1.0f, y + 1 < g.Y ? 1.0f : so, y + 2 < g.Y ? 1.0f : so};
-            float4 o4;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float q[5] = {comp(qd2, k), comp(qd1, k), comp(qc, k), comp(qu1, k), comp(qu2, k)};
-                const float r = ppm_cell(q, o2, comp(vc4, k), comp(vm4, k), dt, vox);
-                if (k == 0) o4.x = r; else if (k == 1) o4.y = r; else if (k == 2) o4.z = r; else o4.w = r;
-            }
-            *reinterpret_cast<float4*>(out + c) = o4;
+        for (int k = 0; k < 4; ++k) {
+            const float u = comp(vc, k);
+            setc(Fp, k, face_flux(u, comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k), cdt));
+            setc(Fpo, k, oin ? u : face_flux(u, oz(z - 1), oz(z), oz(z + 1), oz(z + 2), cdt));
+            setc(o4, k, ppm_update(comp(w2, k), comp(Fp, k), comp(Fc, k), comp(Fpo, k), comp(Fco, k), cdt));
         }
+        *reinterpret_cast<float4*>(out + c) = o4;
+        Fc = Fp;
+        Fco = Fpo;
+        w0 = w1; w1 = w2; w2 = w3; w3 = w4;
     }
 }
 
@@ -585,6 +641,38 @@ __global__ void __launch_bounds__(256) k_new_pressure(Grid g, float* __restrict_
 // Launchers
 // ---------------------------------------------------------------------------------------------
 
+namespace {
+
+// Flat terrain, X % 4 == 0: the sweeps alternate between the scratch fields and the last one
+// writes f itself, so no copy is needed (no sweep reads the array it writes, and the ground rows
+// of the scratch fields are never read). A single sweep goes through a scratch field.
+void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float* def, float k, int sweeps) {
+    const Grid& g = e.g;
+    const int vx = (g.X / 4 + 31) / 32, vy = (g.Y - 1 + DVY - 1) / DVY;
+    int vz = std::max(1, std::min(g.Z, (e.num_sms * 16 + vx * vy - 1) / (vx * vy)));
+    const int vlen = (g.Z + vz - 1) / vz;
+    vz = (g.Z + vlen - 1) / vlen;
+    float* buf[2] = {e.tA, e.tB};
+    const float* src = f;
+    for (int q = 0; q < sweeps; ++q) {
+        float* dst = (q == sweeps - 1 && q > 0) ? f : buf[q % 2];
+        if (type == 0)
+            k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, e.p, e.Tg, e.Pg);
+        else
+            k_diffuse4<false><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, e.p, e.Tg, e.Pg);
+        e.launches += 1;
+        src = dst;
+    }
+    if (sweeps == 1) {
+        const int n4 = g.N / 4;
+        k_copy_sky4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)src, (float4*)f,
+                                                                                     nullptr, 0);
+        e.launches += 1;
+    }
+}
+
+}  // namespace
+
 // diffuseGPU Game/environment.cu:597-673: per-type boundary table :603-638, k = 0.005*dt/vox^2
 void launch_diffuse(Env& e, float* f, int type, float dtS) {
     const Grid& g = e.g;
@@ -601,6 +689,10 @@ void launch_diffuse(Env& e, float* f, int type, float dtS) {
     const float k = 0.005f * dtS / (g.vox * g.vox);
     const int sweeps = e.cfg.diffuse_sweeps;
     ProfScope ps(e, "diffuse");
+    if (e.flat && (g.X % 4) == 0 && sweeps > 0) {
+        diffuse_vec(e, f, type, sides, ground, def, k, sweeps);
+        return;
+    }
     e.launches += sweeps + 1;
     cudaMemcpyAsync(e.tA, f, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
     cudaMemcpyAsync(e.tB, f, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
@@ -679,26 +771,32 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     const int zlen2 = (g.Z + zc2 - 1) / zc2;
     zc2 = (g.Z + zlen2 - 1) / zlen2;
     const dim3 vg2(gx, gy, zc2);
+    // the Y pass marches rows in runs
+    const int ygz = (g.Z + PY - 1) / PY;
+    int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * 16 + gx * ygz - 1) / (gx * ygz)));
+    const int ylen = (g.Y - 1 + yc - 1) / yc;
+    yc = (g.Y - 1 + ylen - 1) / ylen;
+    const dim3 yg(gx, ygz, yc), yb(32, PY);
     const int n4 = g.N / 4;
     const int ncopy = std::min((n4 + 255) / 256, e.num_sms * 8);
     e.launches += 6LL * slots;
     for (int i = 0; i < slots; ++i) {
         if (vec) {
-            k_ppm4<0><<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+            k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
             const float* vy = e.v;
             if (f == e.v) {
                 cudaMemcpyAsync(e.tB, e.v, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
                 vy = e.tB;
             }
-            k_ppm4<1><<<vg, vb, 0, e.stream>>>(g, zlen, O, A, vy, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
-            k_ppm4<2><<<vg2, vb, 0, e.stream>>>(g, zlen2, A, O, e.w, def, sides, ground, e.defU, e.defW, dtS, nsub, 0, chk, i);
+            k_ppm4y<<<yg, yb, 0, e.stream>>>(g, ylen, O, A, vy, def, sides, ground, dtS, nsub, 1, chk, i);
+            k_ppm4z<<<vg2, vb, 0, e.stream>>>(g, zlen2, A, O, e.w, def, sides, e.defW, dtS, nsub, 0, chk, i);
             vy = e.v;
             if (f == e.v) {
                 cudaMemcpyAsync(e.tB, e.v, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
                 vy = e.tB;
             }
-            k_ppm4<1><<<vg, vb, 0, e.stream>>>(g, zlen, O, A, vy, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
-            k_ppm4<0><<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
+            k_ppm4y<<<yg, yb, 0, e.stream>>>(g, ylen, O, A, vy, def, sides, ground, dtS, nsub, 1, chk, i);
+            k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
             k_copy_sky4<<<ncopy, 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)O, (float4*)A, chk, i);
             continue;
         }
