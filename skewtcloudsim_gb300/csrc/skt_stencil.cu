@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) k_diffuse(Grid g, const float* __restrict
             }
         }
     }
-    out[c] = (in[c] + k * (l + r + u + d + f + b)) / (1 + 6 * k);
+    out[c] = (in[c] + k * (l + r + u + d + f + b)) * (1.0f / (1 + 6 * k));
 }
 
 // Vectorised sweep for flat terrain (ground = the y = 0 layer) and X % 4 == 0: four cells per
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const f
     const int row = x0 + y * X;
     const float dy = act ? (def ? def[y] : 0.0f) : 0.0f;
     const float dy0 = def ? def[0] : 0.0f;
-    const float inv = 1 + 6 * k;
+    const float rinv = 1.0f / (1 + 6 * k);
     float4 qb = make_float4(0, 0, 0, 0), qc = qb;
     if (act) {
         qc = ld4f(in, row + zs * XY);
@@ -114,10 +114,10 @@ __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const f
                 qd.w = theta_ground(p, Tg, Pg, c + 3, gi + 3);
             }
             float4 o;
-            o.x = (qc.x + k * (ql + qc.y + qu.x + qd.x + qf.x + qb.x)) / inv;
-            o.y = (qc.y + k * (qc.x + qc.z + qu.y + qd.y + qf.y + qb.y)) / inv;
-            o.z = (qc.z + k * (qc.y + qc.w + qu.z + qd.z + qf.z + qb.z)) / inv;
-            o.w = (qc.w + k * (qc.z + qr + qu.w + qd.w + qf.w + qb.w)) / inv;
+            o.x = (qc.x + k * (ql + qc.y + qu.x + qd.x + qf.x + qb.x)) * rinv;
+            o.y = (qc.y + k * (qc.x + qc.z + qu.y + qd.y + qf.y + qb.y)) * rinv;
+            o.z = (qc.z + k * (qc.y + qc.w + qu.z + qd.z + qf.z + qb.z)) * rinv;
+            o.w = (qc.w + k * (qc.z + qr + qu.w + qd.w + qf.w + qb.w)) * rinv;
             *reinterpret_cast<float4*>(out + c) = o;
         }
         qb = qc;
@@ -125,31 +125,30 @@ __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const f
     }
 }
 
-// advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp).
-// cdt = dt/vox: the Courant number is veli*cdt (the reference divides veli*dt by vox each call)
-// and the limiter ratios use the fast divide; both change results by a few ulp at most.
+// advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp),
+// written without branches: the limiter ratios are formed unconditionally and selected, the
+// parabola's sign case by a select. cdt = dt/vox: the Courant number is veli*cdt (the reference
+// divides veli*dt by vox each call) and the limiter ratios use the fast divide; both change
+// results by a few ulp at most.
 __device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float vR, float cdt) {
-    float C = veli * cdt;
-    C = C > 1.0f ? 1.0f : (C < -1.0f ? -1.0f : C);
+    const float C = fminf(fmaxf(veli * cdt, -1.0f), 1.0f);
     const float qMin = fminf(vL, fminf(vC, vR));
     const float qMax = fmaxf(vL, fmaxf(vC, vR));
-    float s = 0.0f;
-    const float dl = vC - vL, dr = vR - vC;
-    if (dl * dr > 0.0f) {
-        const float db = vR - vL;
-        const float lim = fminf(0.5f * fabsf(db), fminf(fabsf(dr), fabsf(dl)));
-        s = db >= 0.0f ? lim : -lim;
-    }
+    const float dl = vC - vL, dr = vR - vC, db = vR - vL;
+    const float lim = fminf(0.5f * fabsf(db), fminf(fabsf(dr), fabsf(dl)));
+    const float s = dl * dr > 0.0f ? (db >= 0.0f ? lim : -lim) : 0.0f;
     const float qLS = vC - 0.5f * s, qRS = vC + 0.5f * s;
-    float B = 1.0f;
-    if (qRS > qMax) { const float den = qRS - vC; if (den > 1e-16f) B = fminf(B, __fdividef(qMax - vC, den)); }
-    if (qLS < qMin) { const float den = vC - qLS; if (den > 1e-16f) B = fminf(B, __fdividef(vC - qMin, den)); }
+    const float denR = qRS - vC, denL = vC - qLS;
+    const float bR = (qRS > qMax && denR > 1e-16f) ? __fdividef(qMax - vC, denR) : 1.0f;
+    const float bL = (qLS < qMin && denL > 1e-16f) ? __fdividef(vC - qMin, denL) : 1.0f;
+    const float B = fminf(1.0f, fminf(bR, bL));
     float qR = vC + B * (qRS - vC);
     float qL = vC + B * (qLS - vC);
-    if ((qR - vC) * (vC - qL) <= 0.0f) { qR = qL = vC; }
-    float qq;
-    if (C > 0.0f) qq = qR + C * (-qL - 2 * qR + 3 * vC) + C * C * (qL + qR - 2 * vC);
-    else qq = qR + C * (-2 * qL - qR + 3 * vC) + C * C * (qL + qR - 2 * vC);
+    const bool flat = (qR - vC) * (vC - qL) <= 0.0f;
+    qR = flat ? vC : qR;
+    qL = flat ? vC : qL;
+    const float lin = C > 0.0f ? (-qL - 2 * qR + 3 * vC) : (-2 * qL - qR + 3 * vC);
+    const float qq = qR + C * lin + C * C * (qL + qR - 2 * vC);
     return veli * qq;
 }
 
@@ -159,14 +158,15 @@ __device__ __forceinline__ float ppm_flux(float veli, float vL, float vC, float 
 // (the previous cell's velocity, window q-2..q+1 seen from it) are the same call, so each face is
 // computed once and handed on. For a window of ones the flux is exactly u.
 __device__ __forceinline__ float face_flux(float u, float a, float b, float c, float d, float cdt) {
-    return u >= 0.0f ? ppm_flux(u, a, b, c, cdt) : ppm_flux(u, d, c, b, cdt);
+    const bool up = u >= 0.0f;
+    return ppm_flux(u, up ? a : d, up ? b : c, up ? c : b, cdt);
 }
 
 // the advected value over the advected density companion (divideValues Game/kernelMaths.cu:38)
 __device__ __forceinline__ float ppm_update(float q, float fp, float fm, float fpo, float fmo, float cdt) {
     const float nq = q - cdt * (fp - fm);
     const float nr = 1.0f - cdt * (fpo - fmo);
-    return nq / nr;
+    return __fdividef(nq, nr);
 }
 
 // ghost value of the density companion (a field of ones, custom value 1)
@@ -251,9 +251,7 @@ __global__ void __launch_bounds__(32 * DVY) k_ppm4x(Grid g, int zlen, const floa
     const float du = act ? defU[y] : 0.0f;
     const float so = bc_val(sides, 1.0f, 1.0f);
     const bool xedge = x0 < 4 || x0 + 8 > X;  // the companion window reaches outside the domain
-    float ow[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) ow[j] = (x0 - 2 + j >= 0 && x0 - 2 + j < X) ? 1.0f : so;
+    auto ow = [&](int j) { return (x0 - 2 + j >= 0 && x0 - 2 + j < X) ? 1.0f : so; };
     for (int z = zs; z < ze; ++z) {
         const int c = row + z * XY;
         float4 qc = make_float4(0, 0, 0, 0), uc = qc;
@@ -275,13 +273,17 @@ __global__ void __launch_bounds__(32 * DVY) k_ppm4x(Grid g, int zlen, const floa
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             F[k] = face_flux(u[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], cdt);
-            Fo[k] = xedge ? face_flux(u[k], ow[k + 1], ow[k + 2], ow[k + 3], ow[k + 4], cdt) : u[k];
+            Fo[k] = u[k];
+        }
+        if (xedge) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) Fo[k] = face_flux(u[k], ow(k + 1), ow(k + 2), ow(k + 3), ow(k + 4), cdt);
         }
         float Fm = __shfl_up_sync(0xffffffffu, F[3], 1);
         float Fmo = __shfl_up_sync(0xffffffffu, Fo[3], 1);
         if (lane == 0) {
             Fm = face_flux(um1, w[0], w[1], w[2], w[3], cdt);
-            Fmo = xedge ? face_flux(um1, ow[0], ow[1], ow[2], ow[3], cdt) : um1;
+            Fmo = xedge ? face_flux(um1, ow(0), ow(1), ow(2), ow(3), cdt) : um1;
         }
         if (act) {
             float4 o4;
