@@ -118,10 +118,10 @@ __global__ void k_mg_jacobi(LvlView L, const float* __restrict__ in, const float
     const int c = lidx(L, x, y, z);
     const float d = L.aw[c];
     if (d == 0.0f) { out[c] = 0.0f; return; }
-    if (FIRST) { out[c] = b[c] / (kChebTheta * d); return; }
+    if (FIRST) { out[c] = __fdividef(b[c], kChebTheta * d); return; }
     const float v = in[c];
     const float pv = prev ? prev[c] : 0.0f;
-    out[c] = v + c1 * (v - pv) + c2 * (b[c] - apply_A(L, in, x, y, z, c)) / d;
+    out[c] = v + c1 * (v - pv) + c2 * __fdividef(b[c] - apply_A(L, in, x, y, z, c), d);
 }
 
 // coarse right-hand side: the sum of the residuals of the eight children
@@ -152,25 +152,52 @@ __global__ void k_mg_prolong(LvlView F, float* __restrict__ x, int CX, int CY, c
     x[c] += ce[(fx >> 1) + CX * ((fy >> 1) + CY * (fz >> 1))];
 }
 
-// the coarsest level: kCoarseSweeps damped Jacobi sweeps from zero in shared memory, one block
-__global__ void __launch_bounds__(512) k_mg_coarse(LvlView L, const float* __restrict__ b, float* __restrict__ x, const int* skip) {
+// the coarsest level: kCoarseSweeps damped Jacobi sweeps from zero, one block of kCoarseThreads;
+// each thread keeps its (up to kCoarsePer) cells' seven coefficients in registers for all sweeps,
+// the iterate lives in shared memory (a missing neighbour has coefficient 0; its index is only
+// clamped into the level, the value read there is finite and multiplied by 0)
+constexpr int kCoarseThreads = 1024, kCoarsePer = kCoarseMax / kCoarseThreads;
+__global__ void __launch_bounds__(kCoarseThreads) k_mg_coarse(LvlView L, const float* __restrict__ b, float* __restrict__ x, const int* skip) {
     if (skip && *skip) return;
     extern __shared__ float sm[];
-    const int n = L.X * L.Y * L.Z;
+    const int n = L.X * L.Y * L.Z, XY = L.X * L.Y;
     float* xa = sm;
     float* xb = sm + n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) xa[i] = 0.0f;
+    float cw[kCoarsePer], cl[kCoarsePer], cr[kCoarsePer], cd[kCoarsePer], cu[kCoarsePer], cbk[kCoarsePer], cf[kCoarsePer], bv[kCoarsePer];
+    int ci[kCoarsePer];
+#pragma unroll
+    for (int k = 0; k < kCoarsePer; ++k) {
+        const int c = threadIdx.x + k * kCoarseThreads;
+        const bool v = c < n;
+        const int cc = v ? c : 0;
+        const int xx = cc % L.X, yy = (cc / L.X) % L.Y, zz = cc / XY;
+        ci[k] = cc;
+        cw[k] = v ? L.aw[cc] : 0.0f;
+        bv[k] = v ? b[cc] : 0.0f;
+        cl[k] = (v && xx > 0) ? L.ax[cc - 1] : 0.0f;
+        cr[k] = (v && xx + 1 < L.X) ? L.ax[cc] : 0.0f;
+        cd[k] = (v && yy > 0) ? L.ay[cc - L.X] : 0.0f;
+        cu[k] = (v && yy + 1 < L.Y) ? L.ay[cc] : 0.0f;
+        cbk[k] = (v && zz > 0) ? L.az[cc - XY] : 0.0f;
+        cf[k] = (v && zz + 1 < L.Z) ? L.az[cc] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < n; i += kCoarseThreads) xa[i] = 0.0f;
     __syncthreads();
     for (int it = 0; it < kCoarseSweeps; ++it) {
-        for (int c = threadIdx.x; c < n; c += blockDim.x) {
-            const int xx = c % L.X, yy = (c / L.X) % L.Y, zz = c / (L.X * L.Y);
-            const float d = L.aw[c];
-            xb[c] = d == 0.0f ? 0.0f : xa[c] + kOmega * (b[c] - apply_A(L, xa, xx, yy, zz, c)) / d;
+#pragma unroll
+        for (int k = 0; k < kCoarsePer; ++k) {
+            if (threadIdx.x + k * kCoarseThreads >= n) break;
+            const int c = ci[k];
+            const float d = cw[k];
+            const float xc = xa[c];
+            const float ax_ = d * xc + cl[k] * xa[max(c - 1, 0)] + cr[k] * xa[min(c + 1, n - 1)] + cd[k] * xa[max(c - L.X, 0)] +
+                              cu[k] * xa[min(c + L.X, n - 1)] + cbk[k] * xa[max(c - XY, 0)] + cf[k] * xa[min(c + XY, n - 1)];
+            xb[c] = d == 0.0f ? 0.0f : xc + kOmega * __fdividef(bv[k] - ax_, d);
         }
         __syncthreads();
         float* t = xa; xa = xb; xb = t;
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xa[i];
+    for (int i = threadIdx.x; i < n; i += kCoarseThreads) x[i] = xa[i];
 }
 
 // ---- refinement / CG helpers (1D over all cells) ---------------------------------------------
@@ -238,58 +265,97 @@ __device__ __forceinline__ bool finish(Scalars* sc, double* partials, double sum
     return threadIdx.x == 0;
 }
 
-// r32 = b - A x64 in FP64, |r|^2 in FP64; mode 0 records |b|^2 (x64 = 0 on entry)
-__global__ void __launch_bounds__(RT) k_resid64(Grid g, const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ az,
-                                                const float* __restrict__ aw, const double* __restrict__ x, const float* __restrict__ b,
-                                                float* __restrict__ r, float refine_tol, int first, Scalars* sc, double* partials) {
-    __shared__ double smd[RT / 32];
-    double acc = 0.0;
-    float mx = 0.0f;
-    for (int c = blockIdx.x * RT + threadIdx.x; c < g.N; c += gridDim.x * RT) {
-        double rv = 0.0;
-        if (aw[c] != 0.0f) {
-            const int xx = c % g.X, yy = (c / g.X) % g.Y, zz = c / g.XY;
-            double s = double(aw[c]) * x[c];
-            if (xx > 0) s += double(ax[c - 1]) * x[c - 1];
-            if (xx + 1 < g.X) s += double(ax[c]) * x[c + 1];
-            if (yy > 0) s += double(ay[c - g.X]) * x[c - g.X];
-            if (yy + 1 < g.Y) s += double(ay[c]) * x[c + g.X];
-            if (zz > 0) s += double(az[c - g.XY]) * x[c - g.XY];
-            if (zz + 1 < g.Z) s += double(az[c]) * x[c + g.XY];
-            rv = double(b[c]) - s;
-        }
-        r[c] = float(rv);
-        acc += rv * rv;
-        const float m = fabsf(float(rv));
-        if (m > mx) mx = m;
-    }
-    const double bs = bsum<RT>(acc, smd);
-    double tot;
-    float mall;
-    if (finish(sc, partials, bs, mx, tot, mall)) {
-        if (first) sc->rnorm0 = sqrt(tot);
-        sc->rnorm = sqrt(tot);
-        sc->residual = mall;
-        const bool done = sc->rnorm0 == 0.0 || sc->rnorm <= double(refine_tol) * sc->rnorm0;
-        sc->refine_done = done ? 1 : 0;
-        sc->inner_tol = mall;       // the inner solves reduce the max residual relative to this
-    }
+// ---- float-float refinement vector ----------------------------------------------------------
+// The refinement's solution is kept as an unevaluated sum x = xh + xl of two floats (about 48
+// significant bits) and its residual b - A x is formed with error-free transformations (Knuth's
+// two-sum and the fma-based exact product), so the outer loop converges far below FP32 rounding
+// on the FP32 pipes; the FP64 rate of this chip is a small fraction of its FP32 rate.
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bv = s - a;
+    e = (a - (s - bv)) + (b - bv);
 }
 
-// x64 += e (FP64) and e = 0
-__global__ void __launch_bounds__(RT) k_accum64(int n, double* __restrict__ x, float* __restrict__ e) {
+struct FF {  // running float-float sum of products a * (xh + xl)
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void add_prod(float a, float xh, float xl) {
+        const float p = a * xh;
+        const float pe = fmaf(a, xh, -p);  // a*xh - p exactly
+        float sh, se;
+        two_sum(h, p, sh, se);
+        h = sh;
+        l += se + fmaf(a, xl, pe);
+    }
+};
+
+// b - (h + l), rounded once to float
+__device__ __forceinline__ float ff_resid(float b, const FF& acc) {
+    float d, e;
+    two_sum(b, -acc.h, d, e);
+    return d + (e - acc.l);
+}
+
+// the refinement bookkeeping once |r|^2 and max|r| are known (first call: x = 0, r = b)
+__device__ __forceinline__ void refine_record(Scalars* sc, double tot, float mall, float refine_tol, int first) {
+    if (first) sc->rnorm0 = sqrt(tot);
+    sc->rnorm = sqrt(tot);
+    sc->residual = mall;
+    const bool done = sc->rnorm0 == 0.0 || sc->rnorm <= double(refine_tol) * sc->rnorm0;
+    sc->refine_done = done ? 1 : 0;
+    sc->inner_tol = mall;  // the inner solves reduce the max residual relative to this
+}
+
+// r = b - A (xh + xl) in float-float, |r|^2 (compensated FP32 per thread, FP64 across threads)
+// and max|r|; any grid
+__global__ void __launch_bounds__(RT) k_resid_ff(Grid g, const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ az,
+                                                 const float* __restrict__ aw, const float* __restrict__ xh, const float* __restrict__ xl,
+                                                 const float* __restrict__ b, float* __restrict__ r, float refine_tol, int first, Scalars* sc,
+                                                 double* partials) {
+    __shared__ double smd[RT / 32];
+    float acc = 0.0f, comp = 0.0f, mx = 0.0f;
+    for (int c = blockIdx.x * RT + threadIdx.x; c < g.N; c += gridDim.x * RT) {
+        float rv = 0.0f;
+        if (aw[c] != 0.0f) {
+            const int xx = c % g.X, yy = (c / g.X) % g.Y, zz = c / g.XY;
+            FF s;
+            s.add_prod(aw[c], xh[c], xl[c]);
+            if (xx > 0) s.add_prod(ax[c - 1], xh[c - 1], xl[c - 1]);
+            if (xx + 1 < g.X) s.add_prod(ax[c], xh[c + 1], xl[c + 1]);
+            if (yy > 0) s.add_prod(ay[c - g.X], xh[c - g.X], xl[c - g.X]);
+            if (yy + 1 < g.Y) s.add_prod(ay[c], xh[c + g.X], xl[c + g.X]);
+            if (zz > 0) s.add_prod(az[c - g.XY], xh[c - g.XY], xl[c - g.XY]);
+            if (zz + 1 < g.Z) s.add_prod(az[c], xh[c + g.XY], xl[c + g.XY]);
+            rv = ff_resid(b[c], s);
+        }
+        r[c] = rv;
+        const float yv = rv * rv - comp;
+        const float tt = acc + yv;
+        comp = (tt - acc) - yv;
+        acc = tt;
+        mx = fmaxf(mx, fabsf(rv));
+    }
+    const double bs = bsum<RT>(double(acc) - double(comp), smd);
+    double tot;
+    float mall;
+    if (finish(sc, partials, bs, mx, tot, mall)) refine_record(sc, tot, mall, refine_tol, first);
+}
+
+// (xh, xl) += e and e = 0
+__global__ void __launch_bounds__(RT) k_accum_ff(int n, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ e) {
     for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) {
-        x[c] += double(e[c]);
+        float sh, se;
+        two_sum(xh[c], e[c], sh, se);
+        se += xl[c];
+        const float h = sh + se;
+        xh[c] = h;
+        xl[c] = se - (h - sh);
         e[c] = 0.0f;
     }
 }
 
-__global__ void __launch_bounds__(RT) k_zero64(int n, double* __restrict__ x) {
-    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) x[c] = 0.0;
-}
-
-__global__ void __launch_bounds__(RT) k_cast64(int n, const double* __restrict__ x, float* __restrict__ p) {
-    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) p[c] = float(x[c]);
+__global__ void __launch_bounds__(RT) k_cast_ff(int n, const float* __restrict__ xh, const float* __restrict__ xl, float* __restrict__ p) {
+    for (int c = blockIdx.x * RT + threadIdx.x; c < n; c += gridDim.x * RT) p[c] = xh[c] + xl[c];
 }
 
 // inner CG: rho = z.r (FP64) and s = z (start), or beta = rho_new/rho and s = z + beta s
@@ -395,10 +461,16 @@ __device__ __forceinline__ float4 ld4(const __half* p, int c) {
 }
 __device__ __forceinline__ float ld1(const float* p, int c) { return p[c]; }
 __device__ __forceinline__ float ld1(const __half* p, int c) { return __half2float(p[c]); }
+__device__ __forceinline__ float comp4(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+__device__ __forceinline__ void set4(float4& v, int k, float a) {
+    if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
+}
 
 enum { SM_PRE = 0, SM_POSTA = 1, SM_POSTB = 2 };
 enum { DOT_NONE = 0, DOT_START = 1, DOT_NEXT = 2 };
 
+// Divisions by the diagonal use the fast divide: the preconditioner only has to be a fixed
+// symmetric operator, and a deterministic approximate D^-1 keeps it one.
 // The smoother's input vector u as seen by the stencil:
 //   SM_PRE   u = b / (theta diag)       (step A of the Chebyshev smoother from zero, on the fly)
 //   SM_POSTA u = x + P e_coarse         (the coarse correction, injected on the fly)
@@ -415,8 +487,8 @@ struct UIn {
         const float4 a = ld4(v, c);
         if (MODE == SM_PRE) {
             const float4 d = ld4(aw, c);
-            return make_float4(d.x == 0.0f ? 0.0f : a.x / (kChebTheta * d.x), d.y == 0.0f ? 0.0f : a.y / (kChebTheta * d.y),
-                               d.z == 0.0f ? 0.0f : a.z / (kChebTheta * d.z), d.w == 0.0f ? 0.0f : a.w / (kChebTheta * d.w));
+            return make_float4(d.x == 0.0f ? 0.0f : __fdividef(a.x, kChebTheta * d.x), d.y == 0.0f ? 0.0f : __fdividef(a.y, kChebTheta * d.y),
+                               d.z == 0.0f ? 0.0f : __fdividef(a.z, kChebTheta * d.z), d.w == 0.0f ? 0.0f : __fdividef(a.w, kChebTheta * d.w));
         }
         if (MODE == SM_POSTA) {
             const float2 e = *reinterpret_cast<const float2*>(ce + (x0 >> 1) + CX * ((y >> 1) + CY * (z >> 1)));
@@ -428,7 +500,7 @@ struct UIn {
         const float a = v[c];
         if (MODE == SM_PRE) {
             const float d = ld1(aw, c);
-            return d == 0.0f ? 0.0f : a / (kChebTheta * d);
+            return d == 0.0f ? 0.0f : __fdividef(a, kChebTheta * d);
         }
         if (MODE == SM_POSTA) return a + ce[(xx >> 1) + CX * ((y >> 1) + CY * (z >> 1))];
         return a;
@@ -476,6 +548,45 @@ __device__ __forceinline__ bool finish_sum(Scalars* sc, double* partials, double
     return tid == 0;
 }
 
+// finish_sum with a max as well (partials[kMaxPartials + bid] holds the block maxima)
+template <int NTH>
+__device__ __forceinline__ bool finish_sum_max(Scalars* sc, double* partials, double sum, float mx, double& tot, float& mall, int tid) {
+    __shared__ bool last;
+    __shared__ double sd[NTH / 32];
+    __shared__ float sf[NTH / 32];
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nblk = gridDim.x * gridDim.y * gridDim.z;
+    if (tid == 0) {
+        partials[bid] = sum;
+        partials[kMaxPartials + bid] = double(mx);
+        __threadfence();
+        last = atomicAdd(&sc->done_blocks, 1u) == unsigned(nblk) - 1u;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    float m = 0.0f;
+    for (int b = tid; b < nblk; b += NTH) {
+        s += __ldcg(partials + b);
+        m = fmaxf(m, float(__ldcg(partials + kMaxPartials + b)));
+    }
+    const double ts = bsum_t<NTH>(s, sd, tid);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __syncthreads();
+    if ((tid & 31) == 0) sf[tid >> 5] = m;
+    __syncthreads();
+    if (tid == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < NTH / 32; ++w) t = fmaxf(t, sf[w]);
+        tot = ts;
+        mall = t;
+        sc->done_blocks = 0;
+    }
+    return tid == 0;
+}
+
 // (A u) at the four cells of a row from the z-march registers
 struct Stencil4 {
     float4 a;
@@ -494,7 +605,7 @@ struct Stencil4 {
 // being written only). DOT forms z.r (r = b) of the finest level's output for the CG:
 // DOT_START sets sigma0 and restarts the iteration count, DOT_NEXT sets beta = rho_new/rho.
 template <int MODE, int DOT, class CT>
-__global__ void __launch_bounds__(32 * JVY) k_mg_smooth4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
+__global__ void __launch_bounds__(32 * JVY, 8) k_mg_smooth4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
                                                          const CT* __restrict__ az, const CT* __restrict__ aw, const float* __restrict__ b,
                                                          UIn<MODE, CT> U, UIn<SM_POSTA, CT> Pv, float* out, float k1, float k2,
                                                          const int* skip, Scalars* sc, double* partials) {
@@ -533,10 +644,10 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_smooth4(int X, int Y, int Z, in
             const float4 a = Stencil4(cw, cx, cy, ayd, azb, cz, axl, vc, vl, vr, vd, vu, vb, vf).a;
             const float4 pv = MODE == SM_POSTB ? Pv.row(c, x0, y, z) : z4;
             float4 o;
-            o.x = cw.x == 0.0f ? 0.0f : vc.x + k1 * (vc.x - pv.x) + k2 * (bb.x - a.x) / cw.x;
-            o.y = cw.y == 0.0f ? 0.0f : vc.y + k1 * (vc.y - pv.y) + k2 * (bb.y - a.y) / cw.y;
-            o.z = cw.z == 0.0f ? 0.0f : vc.z + k1 * (vc.z - pv.z) + k2 * (bb.z - a.z) / cw.z;
-            o.w = cw.w == 0.0f ? 0.0f : vc.w + k1 * (vc.w - pv.w) + k2 * (bb.w - a.w) / cw.w;
+            o.x = cw.x == 0.0f ? 0.0f : vc.x + k1 * (vc.x - pv.x) + k2 * __fdividef(bb.x - a.x, cw.x);
+            o.y = cw.y == 0.0f ? 0.0f : vc.y + k1 * (vc.y - pv.y) + k2 * __fdividef(bb.y - a.y, cw.y);
+            o.z = cw.z == 0.0f ? 0.0f : vc.z + k1 * (vc.z - pv.z) + k2 * __fdividef(bb.z - a.z, cw.z);
+            o.w = cw.w == 0.0f ? 0.0f : vc.w + k1 * (vc.w - pv.w) + k2 * __fdividef(bb.w - a.w, cw.w);
             *reinterpret_cast<float4*>(out + c) = o;
             if (DOT != DOT_NONE) {
                 const float t = o.x * bb.x + o.y * bb.y + o.z * bb.z + o.w * bb.w;
@@ -572,7 +683,7 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_smooth4(int X, int Y, int Z, in
 // eight children. zlen, the z offset of every block, Y and JVY are even: a thread sums its row's
 // x pairs over two planes, then the even row of each row pair adds its partner's sums.
 template <class CT>
-__global__ void __launch_bounds__(32 * JVY) k_mg_restrict4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
+__global__ void __launch_bounds__(32 * JVY, 8) k_mg_restrict4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
                                                            const CT* __restrict__ az, const CT* __restrict__ aw, const float* __restrict__ x,
                                                            const float* __restrict__ b, int CX, int CY, float* __restrict__ cb, const int* skip) {
     if (skip && *skip) return;
@@ -630,7 +741,7 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_restrict4(int X, int Y, int Z, 
 
 // CG search step fused with the operator: s_new = z + beta s_old (beta = 0: s_new = z, s_old
 // is not read), As = A s_new with the FP32 finest coefficients, s_new.As -> alpha = rho/(s.As)
-__global__ void __launch_bounds__(32 * JVY) k_mg_matvec_search4(int X, int Y, int Z, int zlen, const float* __restrict__ ax,
+__global__ void __launch_bounds__(32 * JVY, 8) k_mg_matvec_search4(int X, int Y, int Z, int zlen, const float* __restrict__ ax,
                                                                 const float* __restrict__ ay, const float* __restrict__ az,
                                                                 const float* __restrict__ aw, const float* __restrict__ zv,
                                                                 const float* __restrict__ sold, float* __restrict__ snew,
@@ -702,6 +813,84 @@ __global__ void __launch_bounds__(32 * JVY) k_mg_matvec_search4(int X, int Y, in
         sc->sigma1 = tot;
         sc->alpha = float(sc->sigma0 / tot);
     }
+}
+
+// r = b - A (xh + xl) in float-float on a vector level: the z march of k_mg_matvec_search4 over
+// the pair (xh, xl), |r|^2 and max|r| reduced as in k_resid_ff
+__global__ void __launch_bounds__(32 * JVY) k_resid_ff4(int X, int Y, int Z, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
+                                                        const float* __restrict__ az, const float* __restrict__ aw, const float* __restrict__ xh,
+                                                        const float* __restrict__ xl, const float* __restrict__ b, float* __restrict__ r,
+                                                        float refine_tol, int first, Scalars* sc, double* partials) {
+    const int lane = threadIdx.x, tid = threadIdx.x + 32 * threadIdx.y;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * JVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, Z);
+    const bool act = x0 < X && y < Y;
+    const int XY = X * Y;
+    const int row = x0 + y * X;
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    float4 hb = z4, hc = z4, lb = z4, lc = z4, azb = z4;
+    if (act) {
+        hc = ld4(xh, row + zs * XY);
+        lc = ld4(xl, row + zs * XY);
+        if (zs > 0) { hb = ld4(xh, row + (zs - 1) * XY); lb = ld4(xl, row + (zs - 1) * XY); azb = ld4(az, row + (zs - 1) * XY); }
+    }
+    float acc = 0.0f, comp = 0.0f, mx = 0.0f;
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 hf = z4, lf = z4, hd = z4, ld = z4, hu = z4, lu = z4, ayd = z4, cx = z4, cy = z4, cz = z4, cw = z4, bb = z4;
+        if (act) {
+            if (z + 1 < Z) { hf = ld4(xh, c + XY); lf = ld4(xl, c + XY); }
+            if (y > 0) { hd = ld4(xh, c - X); ld = ld4(xl, c - X); ayd = ld4(ay, c - X); }
+            if (y + 1 < Y) { hu = ld4(xh, c + X); lu = ld4(xl, c + X); }
+            cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c); bb = ld4(b, c);
+        }
+        float hl = __shfl_up_sync(0xffffffffu, hc.w, 1), ll = __shfl_up_sync(0xffffffffu, lc.w, 1);
+        float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
+        float hr = __shfl_down_sync(0xffffffffu, hc.x, 1), lr = __shfl_down_sync(0xffffffffu, lc.x, 1);
+        if (act && lane == 0) {
+            if (x0 > 0) { hl = xh[c - 1]; ll = xl[c - 1]; axl = ax[c - 1]; } else { hl = 0.0f; ll = 0.0f; axl = 0.0f; }
+        }
+        if (act && (lane == 31 || x0 + 4 >= X)) {
+            if (x0 + 4 < X) { hr = xh[c + 4]; lr = xl[c + 4]; } else { hr = 0.0f; lr = 0.0f; }
+        }
+        if (act) {
+            const float H[6] = {hl, hc.x, hc.y, hc.z, hc.w, hr}, L[6] = {ll, lc.x, lc.y, lc.z, lc.w, lr};
+            const float AXm[4] = {axl, cx.x, cx.y, cx.z}, AXp[4] = {cx.x, cx.y, cx.z, cx.w};
+            float4 o;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float d = comp4(cw, k);
+                float rv = 0.0f;
+                if (d != 0.0f) {
+                    FF sacc;
+                    sacc.add_prod(d, H[k + 1], L[k + 1]);
+                    sacc.add_prod(AXm[k], H[k], L[k]);
+                    sacc.add_prod(AXp[k], H[k + 2], L[k + 2]);
+                    sacc.add_prod(comp4(ayd, k), comp4(hd, k), comp4(ld, k));
+                    sacc.add_prod(comp4(cy, k), comp4(hu, k), comp4(lu, k));
+                    sacc.add_prod(comp4(azb, k), comp4(hb, k), comp4(lb, k));
+                    sacc.add_prod(comp4(cz, k), comp4(hf, k), comp4(lf, k));
+                    rv = ff_resid(comp4(bb, k), sacc);
+                }
+                set4(o, k, rv);
+                const float yv = rv * rv - comp;
+                const float tt = acc + yv;
+                comp = (tt - acc) - yv;
+                acc = tt;
+                mx = fmaxf(mx, fabsf(rv));
+            }
+            *reinterpret_cast<float4*>(r + c) = o;
+        }
+        hb = hc; lb = lc;
+        hc = hf; lc = lf;
+        azb = cz;
+    }
+    __shared__ double smd[JVY];
+    const double bs = bsum_t<32 * JVY>(double(acc) - double(comp), smd, tid);
+    double tot;
+    float mall;
+    if (finish_sum_max<32 * JVY>(sc, partials, bs, mx, tot, mall, tid)) refine_record(sc, tot, mall, refine_tol, first);
 }
 
 // FP16 copies of the finest level's coefficients for the V-cycle. Faces round toward zero; the
@@ -909,7 +1098,7 @@ bool vcycle(Env& e, int l, const float* b, float* x, float* x2, const int* skip,
     const LvlView L = view(e, l);
     if (l == e.mg_levels) {
         const int n = L.X * L.Y * L.Z;
-        k_mg_coarse<<<1, 512, 2 * n * sizeof(float), e.stream>>>(L, b, x, skip);
+        k_mg_coarse<<<1, kCoarseThreads, 2 * n * sizeof(float), e.stream>>>(L, b, x, skip);
         e.launches += 1;
         return false;
     }
@@ -981,14 +1170,15 @@ void mg_solve(Env& e) {
     float* ecor = e.tB;
     float* z0 = (float*)e.rd;
     float* z0b = z0 + size_t(n);
+    float* xh = (float*)e.xd;  // the float-float solution (xh, xl) in the FP64 field's storage
+    float* xl = xh + size_t(n);
     {
         ProfScope ps(e, "mg_setup");
         mg_setup(e);
         cudaMemcpyAsync(bvec, e.r, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, e.stream);
         cudaMemsetAsync(ecor, 0, sizeof(float) * size_t(n), e.stream);
-        k_zero64<<<nb, RT, 0, e.stream>>>(n, e.xd);
+        cudaMemsetAsync(xh, 0, sizeof(float) * 2 * size_t(n), e.stream);
         cudaMemsetAsync(&e.sc->outer_inner_total, 0, sizeof(int), e.stream);
-        e.launches += 1;
     }
     const bool fused = e.mg_levels > 0 && vec_level(e, 0);
     int outer = 0;
@@ -996,7 +1186,13 @@ void mg_solve(Env& e) {
     for (; outer < max_outer; ++outer) {
         {
             ProfScope ps(e, "mg_refine");
-            k_resid64<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, e.xd, bvec, e.r, e.cfg.refine_tol, outer == 0, e.sc, e.partials);
+            if (fused) {
+                const March m = march(e, g.X, g.Y, g.Z);
+                k_resid_ff4<<<m.grid, dim3(32, JVY), 0, e.stream>>>(g.X, g.Y, g.Z, m.zlen, e.ax, e.ay, e.az, e.aw, xh, xl, bvec, e.r,
+                                                                  e.cfg.refine_tol, outer == 0, e.sc, e.partials);
+            } else {
+                k_resid_ff<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, xh, xl, bvec, e.r, e.cfg.refine_tol, outer == 0, e.sc, e.partials);
+            }
             e.launches += 1;
         }
         cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
@@ -1030,7 +1226,7 @@ void mg_solve(Env& e) {
                 if (e.host_sc->converged) break;
             }
             { ProfScope ps(e, "mg_refine");
-              k_accum64<<<nb, RT, 0, e.stream>>>(n, e.xd, ecor);
+              k_accum_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, ecor);
               e.launches += 1; }
             continue;
         }
@@ -1073,10 +1269,10 @@ void mg_solve(Env& e) {
             if (e.host_sc->converged) break;
         }
         { ProfScope ps(e, "mg_refine");
-          k_accum64<<<nb, RT, 0, e.stream>>>(n, e.xd, ecor);
+          k_accum_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, ecor);
           e.launches += 1; }
     }
-    k_cast64<<<nb, RT, 0, e.stream>>>(n, e.xd, e.pp);
+    k_cast_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, e.pp);
     e.launches += 1;
     cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
     cudaStreamSynchronize(e.stream);

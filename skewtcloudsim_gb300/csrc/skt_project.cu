@@ -426,6 +426,8 @@ __device__ __forceinline__ float4 f4zero() { return make_float4(0.0f, 0.0f, 0.0f
 // As = A s and s.As with 4 cells per thread along x and a march along z that keeps the planes
 // z-1, z, z+1 of s and the previous plane's z-coefficient in registers. Neighbours outside the
 // domain read as 0; ground neighbours need no test because their s and coefficients are 0.
+// FLAT: the ground is the row y = 0 only (no heightfield reads).
+template <bool FLAT>
 __global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
                                                  const float* __restrict__ az, const float* __restrict__ aw, const float* __restrict__ s,
                                                  float* __restrict__ As, int reference, Scalars* sc, double* partials) {
@@ -454,7 +456,7 @@ __global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* 
             if (y > 0) { sd = ld4(s, c - X); ayd = ld4(ay, c - X); }
             if (y + 1 < g.Y) su = ld4(s, c + X);
             cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c);
-            gh4 = *reinterpret_cast<const int4*>(g.gh + x0 + z * X);
+            if (!FLAT) gh4 = *reinterpret_cast<const int4*>(g.gh + x0 + z * X);
         }
         // x neighbours through the neighbouring lanes; the warp's edge lanes load them
         float sl = __shfl_up_sync(0xffffffffu, scur.w, 1);
@@ -478,10 +480,14 @@ __global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* 
             o.y = cw.y * scur.y + ((AL1 * scur.x + AD1 * sd.y + AB1 * sb.y + cx.y * scur.z + cy.y * su.y + cz.y * sf.y));
             o.z = cw.z * scur.z + ((AL2 * scur.y + AD2 * sd.z + AB2 * sb.z + cx.z * scur.w + cy.z * su.z + cz.z * sf.z));
             o.w = cw.w * scur.w + ((AL3 * scur.z + AD3 * sd.w + AB3 * sb.w + cx.w * sr + cy.w * su.w + cz.w * sf.w));
-            if (y <= gh4.x) o.x = 0.0f;
-            if (y <= gh4.y) o.y = 0.0f;
-            if (y <= gh4.z) o.z = 0.0f;
-            if (y <= gh4.w) o.w = 0.0f;
+            if (FLAT) {
+                if (y == 0) o = f4zero();
+            } else {
+                if (y <= gh4.x) o.x = 0.0f;
+                if (y <= gh4.y) o.y = 0.0f;
+                if (y <= gh4.z) o.z = 0.0f;
+                if (y <= gh4.w) o.w = 0.0f;
+            }
             *reinterpret_cast<float4*>(As + c) = o;
             acc.add(o.x * scur.x);
             acc.add(o.y * scur.y);
@@ -552,7 +558,10 @@ void launch_matvec_textbook(Env& e, const float* s, float* As) {
     while (gx * gy * zc > kMaxPartials && zc > 1) --zc;
     const int zlen = (g.Z + zc - 1) / zc;
     zc = (g.Z + zlen - 1) / zlen;
-    k_matvec4<<<dim3(gx, gy, zc), mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, s, As, 0, e.sc, e.partials);
+    if (e.flat)
+        k_matvec4<true><<<dim3(gx, gy, zc), mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, s, As, 0, e.sc, e.partials);
+    else
+        k_matvec4<false><<<dim3(gx, gy, zc), mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, s, As, 0, e.sc, e.partials);
     e.launches += 1;
 }
 
@@ -588,7 +597,8 @@ void launch_project(Env& e, float dtS) {
         for (int k = 0; k < n; ++k) {
             if (vec) {
                 { ProfScope ps(e, "pcg_matvec"); e.launches += 1;
-                  k_matvec4<<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
+                  if (e.flat) k_matvec4<true><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials);
+                  else k_matvec4<false><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
                 { ProfScope ps(e, "pcg_update"); e.launches += 1;
                   k_update4<<<nstream, UT, 0, e.stream>>>(n4, g.XY / 4, (const float4*)e.aw, (const float4*)e.s, (const float4*)e.As,
                                                           (float4*)e.pp, (float4*)e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
