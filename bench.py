@@ -2,19 +2,24 @@
 """Throughput of the atmosphere step: cell-steps/s on the precision-form workload.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload precision-512x512x256] [--mode plain|mixed|both]
+                    [--workload precision-512x512x256] [--mode both|plain|mixed]
 
 One step = one environmentGPU::updateGPU of the whole grid (ground, diffusion, PPM advection,
 buoyancy, projection, sedimentation, microphysics). Synthetic seeded soundings stand in for the
 reference's radiosonde input. Every field is larger than L2 (268 MB per field at 512x256x512),
 so timed steps do not reuse L2 contents between steps.
 
-Printed JSON line (rank 0): value = whole-job cell-steps/s with the state resident in HBM
-(CUDA events on the library stream); e2e = the same metric through the C ABI from host
-buffers (init H2D + per-step readback of every prognostic field, as the reference's per-step
-GPUSetEnv does); roofline = the dominant kernel's algorithmic bytes / its event-timed launch
-duration against the measured HBM copy bandwidth; cpu_baseline = the oracle (CPU restatement)
-on the host cores on a bounded sub-box sample.
+Printed JSON line (rank 0): value = whole-job cell-steps/s of the plain method with the
+reference's semantics (the drop-in path, 200 Jacobi-PCG iterations per step) with the state
+resident in HBM (CUDA events on the library stream); "mixed" = the same step with the
+mixed-precision projection (FP32 multigrid-preconditioned CG inside float-float iterative
+refinement to a relative residual of 1e-8) and its speed-up over plain; e2e = the headline
+metric through the C ABI from host buffers (init H2D + per-step readback of every prognostic
+field, as the reference's per-step GPUSetEnv does); roofline = the dominant kernel's algorithmic
+bytes / its event-timed launch duration against the measured HBM copy bandwidth; step_roofline =
+algorithmic bytes of the whole step x cell-steps/s against the same peak; cpu_baseline = the
+oracle (CPU restatement) on the host cores on a bounded sub-box sample (all threads, and one
+thread on a smaller box).
 
 Multi-GPU: the path does not shard (one domain per GPU); N>1 runs N independent replicas, one
 per rank, with no collective on the data path ("replicas only").
@@ -50,6 +55,8 @@ STAGE_BYTES = {
     "eos": 16.0,
     "proj_setup": 48.0,
     "proj_apply": 44.0,
+    "mg_matvec": 32.0,    # z, s_old, ax, ay, az, aw read; s_new, As write
+    "mg_update": 24.0,    # s, As read; e, r read+write
 }
 
 
@@ -132,22 +139,40 @@ def pinned_like(a):
         return np.ascontiguousarray(a), None
 
 
-def cpu_baseline(workload: str, sample_shape, steps: int = 1):
-    """The oracle (CPU restatement of the reference, OpenMP on all host cores) on a sub-box."""
+def cpu_baseline(workload: str, sample_shape, steps: int = 1, threads: int = 0):
+    """The oracle (CPU restatement of the reference, OpenMP over the host cores) on a sub-box."""
     import oracle
     from skewtcloudsim_gb300 import sounding
-    init, dt, speed = sounding.workload(workload, scale=sample_shape)
-    st = oracle.OracleState(init, np.float32)
-    cfg = oracle.Config()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        st.step(cfg, dt, speed)
-    el = time.perf_counter() - t0
+    lib = oracle.lib()
+    full = lib.oc_num_threads()
+    if threads:
+        lib.oc_set_threads(threads)
+    try:
+        init, dt, speed = sounding.workload(workload, scale=sample_shape)
+        st = oracle.OracleState(init, np.float32)
+        cfg = oracle.Config()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            st.step(cfg, dt, speed)
+        el = time.perf_counter() - t0
+        used = lib.oc_num_threads()
+    finally:
+        lib.oc_set_threads(full)
     cells = init.nx * init.ny * init.nz
-    return {"value": cells * steps / el, "unit": "cell-steps/s", "cores": oracle.lib().oc_num_threads(),
-            "kind": "port",
+    return {"value": cells * steps / el, "unit": "cell-steps/s", "cores": used, "kind": "port",
             "sample": f"{steps} step(s) of the same workload on a {sample_shape[0]}x{sample_shape[1]}x{sample_shape[2]} "
-                      f"(x,y,z; z vertical) sub-box, reference semantics, FP32, {el:.1f} s"}
+                      f"(x,y,z; z vertical) sub-box, reference semantics, FP32, {used} thread(s), {el:.1f} s"}
+
+
+def host_cpu():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part", "hardware")):
+                    return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
 
 
 def run_reference(args, rank, world):
@@ -173,6 +198,59 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def step_bytes(mode, pcg_iters, outer):
+    """Algorithmic bytes per cell-step of the whole step (FP32, one advection substep): the stage
+    total of the hot-path scope (2558 B) plus the pressure solve. Plain Jacobi-PCG: 52 B per
+    iteration. Mixed: per inner iteration the operator + search (32 B), the update (24 B) and the
+    V-cycle (93 B: four finest-level passes of 16-24.5 B with FP16 coefficients plus the coarser
+    levels), per refinement step the float-float residual (32 B) and the correction (20 B)."""
+    if mode == "plain":
+        return 2558.0 + 52.0 * pcg_iters
+    return 2558.0 + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
+
+
+def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
+    from skewtcloudsim_gb300 import Environment, SolverConfig
+    sem = args.semantics if mode == "plain" else 1
+    cfg = SolverConfig(semantics=sem, precision=1 if mode == "mixed" else 0, mg_half=args.mg_half)
+    env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
+    env.init_from(init)
+    for _ in range(args.warmup):
+        env.update_gpu(dt, speed)
+    env.sync()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region (CUDA events on the library's stream) ---------------
+    barrier()
+    l0 = env.stats()["kernel_launches"]
+    with ClockSampler(local) as clk:
+        env.update_gpu(dt, speed, nsteps=args.steps)
+        barrier()
+    st = env.stats()
+    ms_total = st["gpu_ms"]
+    launches = st["kernel_launches"] - l0
+    if pg:
+        t = torch.tensor([ms_total], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_per_step = ms_total / args.steps
+    value = cells * args.steps * world / (ms_total / 1e3)
+    # ---- per-stage profile of one more step (not timed) ----------------------------------
+    env.profile(True)
+    env.update_gpu(dt, speed)
+    prof = env.profile_read()
+    env.profile(False)
+    sd = env.stats()
+    env.close()
+    return {"mode": mode, "semantics": "reference" if sem == 0 else "textbook", "value": value, "ms_per_step": ms_per_step,
+            "launches": int(launches), "clocks": clk.summary(), "prof": prof, "pcg_iters": sd["pcg_iters"],
+            "outer": sd.get("outer_iters", 0), "converged": sd["converged"], "residual": sd["pcg_residual"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -180,7 +258,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="precision-512x512x256")
-    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--mode", default="both", choices=["plain", "mixed", "both"],
+                    help="both: plain (reference semantics, the headline) and mixed (reported beside it)")
     ap.add_argument("--semantics", type=int, default=0)
     ap.add_argument("--mg-half", type=int, default=1, help="mixed: FP16 finest-level coefficients in the V-cycle")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -203,43 +282,13 @@ def main():
 
     shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
     init, dt, speed = sounding.workload(args.workload, scale=shape)
-    cfg = SolverConfig(semantics=args.semantics, precision=1 if args.mode == "mixed" else 0, mg_half=args.mg_half)
-    env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
-    env.init_from(init)
     cells = init.nx * init.ny * init.nz
+    modes = ["plain", "mixed"] if args.mode == "both" else [args.mode]
+    res = {m: run_mode(args, m, init, dt, speed, cells, world, local, pg, torch) for m in modes}
+    head = res[modes[0]]
+    prof = head["prof"]
 
-    for _ in range(args.warmup):
-        env.update_gpu(dt, speed)
-    env.sync()
-
-    def barrier():
-        if pg:
-            pg.barrier()
-        torch.cuda.synchronize()
-
-    # ---- device-resident timed region ----------------------------------------------------
-    barrier()
-    l0 = env.stats()["kernel_launches"]
-    iters = []
-    with ClockSampler(local) as clk:
-        env.update_gpu(dt, speed, nsteps=args.steps)
-        barrier()
-    st = env.stats()
-    ms_total = st["gpu_ms"]
-    launches = st["kernel_launches"] - l0
-    if pg:
-        t = torch.tensor([ms_total], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_per_step = ms_total / args.steps
-    value = cells * args.steps * world / (ms_total / 1e3)
-
-    # ---- per-stage profile of one more step (not timed) ----------------------------------
-    env.profile(True)
-    env.update_gpu(dt, speed)
-    prof = env.profile_read()
-    env.profile(False)
-    pcg_iters = env.stats()["pcg_iters"]
+    # ---- roofline of the dominant kernel (live CUDA-event timing of its launches) --------
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
     dname, d = dom
     per_launch_ms = d["ms"] / max(d["kernels"], 1)
@@ -250,16 +299,23 @@ def main():
         achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
         roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "traffic": None, "kernel": dname,
-                    "bytes_per_cell": bpc, "peak_source": peak_kind}
+                    "bytes_per_cell": bpc, "launch_us": round(per_launch_ms * 1e3, 2), "peak_source": peak_kind}
     step_ms_prof = sum(v["ms"] for v in prof.values())
+    bstep = step_bytes(head["mode"], head["pcg_iters"], head["outer"])
+    step_model = {"bytes_per_cell_step": bstep, "achieved_gbs": round(bstep * head["value"] / 1e9, 1),
+                  "frac": round(bstep * head["value"] / 1e9 / peak, 4), "peak_source": peak_kind}
 
-    # ---- end to end through the C ABI from host buffers ----------------------------------
+    # ---- end to end through the C ABI from host buffers (headline mode) -------------------
     e2e = None
     if not args.no_e2e and rank == 0:
+        import ctypes
+        import skewtcloudsim_gb300 as pkg
         names = ("th", "qv", "qw", "qc", "qr", "qs", "qi", "u", "v", "w", "p")
         host_in = {k: pinned_like(getattr(init, k)) for k in ("theta", "vel", "qv", "ground_T", "ground_p", "p3d",
                                                                "p_column")}
         outs = {k: pinned_like(np.empty(cells, np.float32)) for k in names}
+        sem = args.semantics if head["mode"] == "plain" else 1
+        cfg = SolverConfig(semantics=sem, precision=1 if head["mode"] == "mixed" else 0, mg_half=args.mg_half)
         env2 = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
         K = args.steps
         torch.cuda.synchronize()
@@ -270,9 +326,8 @@ def main():
             env2.update_gpu(dt, speed)
             for k in names:
                 a = outs[k][0]
-                prm, dr = __import__("skewtcloudsim_gb300").FIELDS[k]
-                env2._check(env2._L.skt_read_field(env2._h, int(prm), int(dr),
-                                                   a.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_float)),
+                prm, dr = pkg.FIELDS[k]
+                env2._check(env2._L.skt_read_field(env2._h, int(prm), int(dr), a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
                                                    a.size))
         el = time.perf_counter() - t0
         h2d = sum(a[0].nbytes for a in host_in.values()) + init.ground_height.nbytes
@@ -286,20 +341,33 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(args.workload, (128, 128, 64), 1)
+        one = cpu_baseline(args.workload, (64, 64, 32), 1, threads=1)
+        cpu["single_thread"] = {"value": one["value"], "sample": one["sample"]}
+        cpu["host"] = {"nproc": os.cpu_count(), "cpu": host_cpu()}
 
-    out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+    field_mb = cells * 4 / 1e6
+    out = {"metric": METRIC, "value": head["value"], "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": args.workload, "grid_xyz": [init.nx, init.nz, init.ny], "cells": cells,
-                      "dt": dt, "pcg": args.mode, "semantics": "reference" if args.semantics == 0 else "textbook",
-                      "pcg_iters_per_step": pcg_iters, "l2": "inputs larger than L2 (268 MB per field)",
+                      "dt": dt, "pcg": head["mode"], "semantics": head["semantics"],
+                      "pcg_iters_per_step": head["pcg_iters"],
+                      "l2": (f"inputs larger than L2 ({field_mb:.0f} MB per field, L2 129 MB)" if field_mb > 129
+                             else f"fields of {field_mb:.0f} MB fit in L2 (129 MB): timings include L2 reuse"),
                       "parallelism": "replicas" if world > 1 else "single"},
-           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-           "clocks": clk.summary(), "profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
-           "profile_step_ms": round(step_ms_prof, 3)}
+           "roofline": roofline, "step_roofline": step_model, "cpu_baseline": cpu, "e2e": e2e,
+           "gpu_launches": head["launches"], "clocks": head["clocks"],
+           "profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "profile_step_ms": round(step_ms_prof, 3)}
+    if "mixed" in res and head["mode"] != "mixed":
+        m = res["mixed"]
+        out["mixed"] = {"value": m["value"], "ms_per_step": m["ms_per_step"], "speedup_vs_plain": round(m["value"] / head["value"], 3),
+                        "semantics": m["semantics"], "inner_iters_per_step": m["pcg_iters"], "refine_steps": m["outer"],
+                        "converged": m["converged"], "rel_residual": m["residual"], "gpu_launches": m["launches"],
+                        "step_roofline": {"bytes_per_cell_step": step_bytes("mixed", m["pcg_iters"], m["outer"]),
+                                          "frac": round(step_bytes("mixed", m["pcg_iters"], m["outer"]) * m["value"] / 1e9 / peak, 4)},
+                        "clocks": m["clocks"], "profile_ms": {k: round(v["ms"], 3) for k, v in m["prof"].items()}}
     if rank == 0:
         print(json.dumps(out), flush=True)
-    env.close()
     if pg:
         pg.destroy_process_group()
 

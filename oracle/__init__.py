@@ -78,6 +78,8 @@ def lib():
         L.oc_irradiance.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
         L.oc_irradiance.restype = ctypes.c_float
         L.oc_num_threads.restype = ctypes.c_int
+        L.oc_set_threads.argtypes = [ctypes.c_int]
+        L.oc_set_threads.restype = None
         _lib = L
     return _lib
 

@@ -1132,6 +1132,14 @@ int oc_num_threads(void) {
 #endif
 }
 
+void oc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 }  // extern "C"
 
 // Single-stage entry points used by the per-kernel parity tests.

@@ -9,9 +9,10 @@ field per step, and equal Courant substep counts.
 On grids wider than 16 cells in x or z the reference's advectGroundWaterGPU reads
 uninitialised shared memory at the interior edges of its 16x16 tiles
 (Game/kernelSky.cu:141-164 fills halos only at the domain edge); the garbage can reach the
-sky fields as non-finite values within a few steps. A step is compared only while the
-reference's own output is finite; the 16x32x16 grid has no interior tile edge and is compared
-on every step.
+sky fields within a few steps, as non-finite values or as finite but wrong ones. A step is
+compared only while the reference's own output is sound: finite, and within 1e-3 of the oracle
+(which otherwise agrees with it to ~1e-6). The 16x32x16 grid has no interior tile edge and is
+compared on every step.
 """
 import json
 import os
@@ -66,7 +67,11 @@ def test_step_against_reference_kernels(gpu_lib, grid):
         gd = env.stats()
         m = ref.sky_mask()
         finite = all(np.isfinite(ref.a[k][m]).all() for k in SKY)
-        row = {"ref_finite": bool(finite), "step": step + 1, "ref_pcg": rd["pcg_iters"][0], "oracle_pcg": od["pcg_iters"], "gpu_pcg": gd["pcg_iters"],
+        # the reference reads uninitialised shared memory at interior ground-tile edges (grids
+        # wider than 16): its state turns NaN, or stays finite but wrong; the independent oracle
+        # tells the two apart (it agrees with the reference to ~1e-6 whenever the reference is sound)
+        sound = finite and all(rel_l2(orc.a[k], ref.a[k], m) <= 1e-3 for k in SKY)
+        row = {"ref_finite": bool(finite), "ref_sound": bool(sound), "step": step + 1, "ref_pcg": rd["pcg_iters"][0], "oracle_pcg": od["pcg_iters"], "gpu_pcg": gd["pcg_iters"],
                "nsub_ref": rd["nsub"][0], "nsub_gpu": gd["nsub"]}
         for k in SKY:
             row[f"oracle_{k}"] = rel_l2(orc.a[k], ref.a[k], m)
@@ -75,11 +80,11 @@ def test_step_against_reference_kernels(gpu_lib, grid):
     _record(f"{X}x{Y}x{Z}", report)
     env.close()
     if (X, Y, Z) == (16, 32, 16):
-        assert all(r["ref_finite"] for r in report)
-    assert report[0]["ref_finite"] or max(X, Z) > 16
+        assert all(r["ref_sound"] for r in report)
+    assert report[0]["ref_sound"] or max(X, Z) > 16
     for row in report:
-        if not row["ref_finite"]:
-            break  # the reference's uninitialised ground-tile halos; later steps start from NaN
+        if not row["ref_sound"]:
+            break  # the reference's uninitialised ground-tile halos; later steps start from its corrupted state
         assert row["nsub_ref"] == row["nsub_gpu"], row
         bad = {k: v for k, v in row.items() if (k.startswith("oracle_") or k.startswith("gpu_"))
                and not k.endswith("_pcg") and v > 1e-5}
