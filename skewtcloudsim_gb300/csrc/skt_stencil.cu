@@ -166,7 +166,7 @@ __device__ __forceinline__ float face_flux(float u, float a, float b, float c, f
 __device__ __forceinline__ float ppm_update(float q, float fp, float fm, float fpo, float fmo, float cdt) {
     const float nq = q - cdt * (fp - fm);
     const float nr = 1.0f - cdt * (fpo - fmo);
-    return __fdividef(nq, nr);
+    return nq / nr;
 }
 
 // ghost value of the density companion (a field of ones, custom value 1)
