@@ -177,6 +177,33 @@ skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, int field_ty
                                const float* default_column_dev, const float* p_dev, const float* ground_T_dev,
                                const float* ground_p_dev, void* stream);
 
+/* ---- Diagnostics (the reference's data graph and debug views) ---------------------------- */
+
+/* Region-summed microphysics process amounts: the reference's data graph
+ * (Game/microPhysics.cu:1356-1413, reset each step at Game/environment.cu:571, read back by
+ * dataClass::setMicroPhysicsData Game/dataClass.cu:42). While enabled, every step sums over the
+ * sky cells with lo <= (x, y, z) <= hi (inclusive, reference layout, y vertical) the 33 amounts
+ * of each cell after its update, PVCON and PVDEP split by sign into PVCON/PVVAP and PVDEP/PVSUB,
+ * PGWET times WTerm and PGDRY times (1 - WTerm); the reference sums with float atomics, here in
+ * FP64. enable = 0 turns it off. The first enable allocates 33 doubles on the device. */
+#define SKT_RATE_COUNT 33
+/* PVCON PVDEP PIMLT PIDW PIHOM PIACR PRACI PRAUT PRACW PREVP PRACS PSACW PSACR PSACI PSAUT PSFW
+ * PSFI PSDEP PSSUB PSMLT PGAUT PGFR PGACW PGACI PGACR PGDRY PGACS PGSUB PGMLT PGWET PGACR1 PVVAP
+ * PVSUB (the order of microPhysicsParams, Game/microPhysics.cuh:7-21) */
+skt_status skt_set_rate_region(skt_env* env, int enable, const int lo[3], const int hi[3]);
+
+/* The region sums of the last step (n must be SKT_RATE_COUNT). Synchronous. */
+skt_status skt_read_rates(skt_env* env, float* host_dst, size_t n);
+
+/* Debug fields, read with skt_read_field / skt_field_device_ptr as the reference's editor reads
+ * its three debug arrays (Game/editor.cpp:190-224, shown as DEBUG1..3): SKT_DEBUG1 is never
+ * written by the reference's GPU step and reads as zeros; SKT_DEBUG2 is buoyancyGPU's velocity
+ * change per sky cell (Game/kernelSky.cu:1128,1244; 0 where no side neighbour is sky), produced
+ * while SKT_DIAG_BUOYANCY is set; SKT_DEBUG3 is the projection's pressure correction
+ * (Game/environment.cu:883). Enabling allocates the debug arrays; a step allocates nothing. */
+#define SKT_DIAG_BUOYANCY 1
+skt_status skt_set_diagnostics(skt_env* env, int flags);
+
 /* Text of the last error on env (or, when env is NULL, of the last skt_create or
  * skt_diffuse_noalloc failure on this thread). */
 const char* skt_last_error(const skt_env* env);

@@ -75,6 +75,12 @@ def lib():
                           ctypes.POINTER(OcState), ctypes.c_int, ctypes.c_int, ctypes.c_float,
                           ctypes.c_float, ctypes.POINTER(OcDiag)]
             f.restype = ctypes.c_int
+        L.oc_micro_rates_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_float,
+                                         ctypes.c_float, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+        L.oc_micro_rates_f32.restype = ctypes.c_int
+        L.oc_buoyancy_dbg_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_float,
+                                          ctypes.POINTER(ctypes.c_float)]
+        L.oc_buoyancy_dbg_f32.restype = ctypes.c_int
         L.oc_irradiance.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
         L.oc_irradiance.restype = ctypes.c_float
         L.oc_num_threads.restype = ctypes.c_int
@@ -160,6 +166,23 @@ class OracleState:
         if rc != 0:
             raise RuntimeError(f"oracle stage failed: {rc}")
         return {"pcg_iters": d.pcg_iters, "pcg_residual": d.pcg_residual, "nsub": d.nsub[0]}
+
+    def micro_rates(self, dt: float, speed: float, lo, hi):
+        """The microphysics stage (FP32 state) and the 33 region-summed process amounts."""
+        assert self.dtype == np.float32
+        st = self._cstate()
+        reg = (ctypes.c_int * 6)(*lo, *hi)
+        out = (ctypes.c_double * 33)()
+        lib().oc_micro_rates_f32(self.X, self.Y, self.Z, ctypes.byref(st), dt, speed, reg, out)
+        return np.array(out[:], np.float64)
+
+    def buoyancy_debug(self, dt: float):
+        """The buoyancy stage (FP32 state) and its per-cell velocity change (0 in ground cells)."""
+        assert self.dtype == np.float32
+        dbg = np.zeros(self.X * self.Y * self.Z, np.float32)
+        st = self._cstate()
+        lib().oc_buoyancy_dbg_f32(self.X, self.Y, self.Z, ctypes.byref(st), dt, dbg.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        return dbg
 
     def sky_mask(self):
         y = np.arange(self.Y)[None, :, None]

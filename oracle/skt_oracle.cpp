@@ -352,7 +352,9 @@ void advect_precip(const Grid& g, const Config& cfg, State<T>& s, T* q, int type
 }
 
 // buoyancyGPU, Game/kernelSky.cu:1061-1247 (bounds DIRICHLET everywhere, Game/environment.cu:1056)
-template <class T> void buoyancy(const Grid& g, State<T>& s, T dt) {
+// dbg (optional): the velocity change of each sky cell, 0 where no neighbour is sky (the
+// reference's buoyancyStor, shown as its second debug field)
+template <class T> void buoyancy(const Grid& g, State<T>& s, T dt, T* dbg = nullptr) {
     const Bounds b{DIRICHLET, DIRICHLET};
     const T kap = kappa<T>();
     const T gg = K<T>::g;
@@ -373,7 +375,10 @@ template <class T> void buoyancy(const Grid& g, State<T>& s, T dt) {
                 auto valid = [&](int dx, int dz) { return g.inside(x + dx, y, z + dz) && !g.ground(x + dx, y, z + dz); };
                 const bool l = valid(-1, 0), r = valid(1, 0), bb = valid(0, -1), f = valid(0, 1);
                 const int nv = int(l) + int(r) + int(bb) + int(f);
-                if (nv == 0) continue;
+                if (nv == 0) {
+                    if (dbg) dbg[idx] = 0;
+                    continue;
+                }
                 auto Q = [&](int dx, int dy, int dz) { return ghost(g, s.qv, x + dx, y + dy, z + dz, b, s.isenQv); };
                 auto TH = [&](int dx, int dy, int dz) { return ghost(g, s.th, x + dx, y + dy, z + dz, b, s.isenT); };
                 const T QP = s.qv[idx];
@@ -417,6 +422,7 @@ template <class T> void buoyancy(const Grid& g, State<T>& s, T dt) {
                 else if (vel < T(0)) fin = BDown;
                 T change = fin * dt;
                 if ((up && vel > T(0) && -change > vel) || (down && vel < T(0) && -change < vel)) change = -vel;
+                if (dbg) dbg[idx] = change;
                 s.v[idx] = vel + change;
             }
 }
@@ -632,9 +638,21 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
 // Sky microphysics + latent heat: calculateEnvMicroPhysicsGPU Game/microPhysics.cu:1035-1354
 // followed by addHeatGPU Game/kernelSky.cu:1249-1282 (both over sky cells).
 // ---------------------------------------------------------------------------------------------
-template <class T> void microphysics_sky(const Grid& g, State<T>& s, T dt, T speed, const Micro<T>& M) {
+// Region-summed process amounts (Game/microPhysics.cu:1356-1413, the data graph): for the sky
+// cells with lo <= (x, y, z) <= hi the 33 values of each cell after its update, PVCON and PVDEP
+// split by sign into PVCON/PVVAP and PVDEP/PVSUB, PGWET times WTerm and PGDRY times (1 - WTerm),
+// summed in double. Order: PVCON PVDEP PIMLT PIDW PIHOM PIACR PRACI PRAUT PRACW PREVP PRACS PSACW
+// PSACR PSACI PSAUT PSFW PSFI PSDEP PSSUB PSMLT PGAUT PGFR PGACW PGACI PGACR PGDRY PGACS PGSUB PGMLT
+// PGWET PGACR1 PVVAP PVSUB.
+struct RateRegion {
+    int lo[3], hi[3];
+    double sums[33];
+};
+
+template <class T> void microphysics_sky(const Grid& g, State<T>& s, T dt, T speed, const Micro<T>& M, RateRegion* rr = nullptr) {
     const T kap = kappa<T>();
-#pragma omp parallel for collapse(2) schedule(static)
+    double acc[33] = {0};
+#pragma omp parallel for collapse(2) schedule(static) reduction(+ : acc[:33])
     for (int z = 0; z < g.Z; ++z)
         for (int y = 0; y < g.Y; ++y)
             for (int x = 0; x < g.X; ++x) {
@@ -758,6 +776,13 @@ template <class T> void microphysics_sky(const Grid& g, State<T>& s, T dt, T spe
                     s.qs[idx] += -PSMLT - PGACS;
                     s.qi[idx] += -PGMLT + PGACS;
                 }
+                if (rr && x >= rr->lo[0] && x <= rr->hi[0] && y >= rr->lo[1] && y <= rr->hi[1] && z >= rr->lo[2] && z <= rr->hi[2]) {
+                    const T PVVAP = PVCON < 0 ? -PVCON : T(0), PVSUB = PVDEP < 0 ? -PVDEP : T(0);
+                    const T v[33] = {PVCON < 0 ? T(0) : PVCON, PVDEP < 0 ? T(0) : PVDEP, PIMLT, PIDW, PIHOM, PIACR, PRACI, PRAUT, PRACW,
+                                     PREVP, PRACS, PSACW, PSACR, PSACI, PSAUT, PSFW, PSFI, PSDEP, PSSUB, PSMLT, PGAUT, PGFR, PGACW,
+                                     PGACI, PGACR, PGDRY * (1 - WT), PGACS, PGSUB, PGMLT, PGWET * WT, PGACR1, PVVAP, PVSUB};
+                    for (int k = 0; k < 33; ++k) acc[k] += double(v[k]);
+                }
                 // addHeatGPU with the updated Qv
                 const T qv2 = s.qv[idx];
                 const T Mair = T(0.02896), Mwat = T(0.01802);
@@ -773,6 +798,8 @@ template <class T> void microphysics_sky(const Grid& g, State<T>& s, T dt, T spe
                 sum += K<T>::Lf / cpth * freeze;
                 s.th[idx] += sum;
             }
+    if (rr)
+        for (int k = 0; k < 33; ++k) rr->sums[k] = acc[k];
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1186,5 +1213,24 @@ int oc_stage_f32(const oc_config* c, int X, int Y, int Z, oc_state* st, int stag
 }
 int oc_stage_f64(const oc_config* c, int X, int Y, int Z, oc_state* st, int stage, int arg, float dt, float speed, oc_diag* d) {
     return stage_impl<double>(c, X, Y, Z, st, stage, arg, dt, speed, d);
+}
+
+// the microphysics stage with the region-summed process amounts (region: lo x,y,z then hi x,y,z)
+int oc_micro_rates_f32(int X, int Y, int Z, oc_state* st, float dt, float speed, const int* region, double* out) {
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    static const Micro<float> M;
+    RateRegion rr{{region[0], region[1], region[2]}, {region[3], region[4], region[5]}, {0}};
+    microphysics_sky(g, s, dt, speed, M, &rr);
+    for (int k = 0; k < 33; ++k) out[k] = rr.sums[k];
+    return 0;
+}
+
+// the buoyancy stage with its per-cell velocity change in dbg
+int oc_buoyancy_dbg_f32(int X, int Y, int Z, oc_state* st, float dt, float* dbg) {
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    buoyancy(g, s, dt, dbg);
+    return 0;
 }
 }  // extern "C"

@@ -5,8 +5,8 @@ include/skewt.h). This package holds the host-side mirror of the reference's env
 (``Environment``), the synthetic sounding generator and the build recipe.
 """
 from .environment import (Environment, SolverConfig, Parameter, Direction, Ground, Column, Status,
-                          SktError, FIELDS, GROUND_FIELDS, COLUMNS)
+                          SktError, FIELDS, GROUND_FIELDS, COLUMNS, DIAG_BUOYANCY, RATE_NAMES)
 from . import sounding
 
 __all__ = ["Environment", "SolverConfig", "Parameter", "Direction", "Ground", "Column", "Status", "SktError",
-           "FIELDS", "GROUND_FIELDS", "COLUMNS", "sounding"]
+           "FIELDS", "GROUND_FIELDS", "COLUMNS", "DIAG_BUOYANCY", "RATE_NAMES", "sounding"]

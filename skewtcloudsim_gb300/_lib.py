@@ -57,6 +57,10 @@ SIGNATURES = {
                                            ctypes.c_float, ctypes.c_int, c_float_p, c_float_p,
                                            ctypes.POINTER(ctypes.c_int32), c_float_p, c_float_p, c_float_p, c_float_p,
                                            ctypes.c_void_p]),
+    "skt_set_rate_region": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)]),
+    "skt_read_rates": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_size_t]),
+    "skt_set_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "skt_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "skt_version": (ctypes.c_char_p, []),
 }

@@ -68,6 +68,9 @@ float* sky_ptr(Env& e, int param, int dir) {
             return nullptr;
         case SKT_PRESSURE: return e.p;
         case SKT_DENSITY: return e.rho;
+        case SKT_DEBUG1: return e.dbg_zero;
+        case SKT_DEBUG2: return e.dbg_buoy;
+        case SKT_DEBUG3: return e.pp;  // the projection's correction, left in pp by every step
         default: return nullptr;
     }
 }
@@ -160,6 +163,61 @@ void skt_default_config(skt_solver_cfg* c) {
     c->inner_rtol = 1e-4f;
     c->use_graph = 0;
     c->mg_half = 1;
+}
+
+skt_status skt_set_rate_region(skt_env* env, int enable, const int lo[3], const int hi[3]) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (!enable) {
+        e.rates_on = 0;
+        return SKT_OK;
+    }
+    if (!lo || !hi) return fail(&e, SKT_INVALID_ARG, "null region bounds");
+    if (!e.rates_dev) {
+        if (cudaMalloc(&e.rates_dev, sizeof(double) * SKT_RATE_COUNT) != cudaSuccess) {
+            cudaGetLastError();
+            e.rates_dev = nullptr;
+            return fail(&e, SKT_OUT_OF_MEMORY, "rate accumulator allocation failed");
+        }
+        cudaMemsetAsync(e.rates_dev, 0, sizeof(double) * SKT_RATE_COUNT, e.stream);
+    }
+    for (int k = 0; k < 3; ++k) {
+        e.rate_lo[k] = lo[k];
+        e.rate_hi[k] = hi[k];
+    }
+    e.rates_on = 1;
+    return cuda_check(e, "set_rate_region");
+}
+
+skt_status skt_read_rates(skt_env* env, float* dst, size_t n) {
+    if (!env || !dst) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    if (n != SKT_RATE_COUNT) return fail(&e, SKT_INVALID_ARG, "n must be SKT_RATE_COUNT");
+    if (!e.rates_dev) return fail(&e, SKT_INVALID_ARG, "the rate region was never enabled");
+    double h[SKT_RATE_COUNT];
+    cudaMemcpyAsync(h, e.rates_dev, sizeof(h), cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    for (size_t k = 0; k < n; ++k) dst[k] = float(h[k]);
+    return cuda_check(e, "read_rates");
+}
+
+skt_status skt_set_diagnostics(skt_env* env, int flags) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (flags & ~SKT_DIAG_BUOYANCY) return fail(&e, SKT_INVALID_ARG, "unknown diagnostics flag");
+    const size_t bytes = sizeof(float) * size_t(e.g.N);
+    if ((flags & SKT_DIAG_BUOYANCY) && !e.dbg_buoy) {
+        if (cudaMalloc(&e.dbg_buoy, bytes) != cudaSuccess || cudaMalloc(&e.dbg_zero, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            if (e.dbg_buoy) cudaFree(e.dbg_buoy);
+            e.dbg_buoy = nullptr;
+            return fail(&e, SKT_OUT_OF_MEMORY, "debug field allocation failed");
+        }
+        cudaMemsetAsync(e.dbg_buoy, 0, bytes, e.stream);
+        cudaMemsetAsync(e.dbg_zero, 0, bytes, e.stream);
+    }
+    e.diag_flags = flags;
+    return cuda_check(e, "set_diagnostics");
 }
 
 const char* skt_version(void) { return "skewt-gb300 0.1 (sm_103a)"; }
@@ -276,6 +334,9 @@ void skt_destroy(skt_env* env) {
     if (e.ev1) cudaEventDestroy(e.ev1);
     if (e.pool) cudaFree(e.pool);
     if (e.mg_pool) cudaFree(e.mg_pool);
+    if (e.rates_dev) cudaFree(e.rates_dev);
+    if (e.dbg_buoy) cudaFree(e.dbg_buoy);
+    if (e.dbg_zero) cudaFree(e.dbg_zero);
     if (e.host_sc) cudaFreeHost(e.host_sc);
     if (e.stream) cudaStreamDestroy(e.stream);
     delete env;
@@ -354,6 +415,8 @@ skt_status skt_read_field(skt_env* env, int param, int dir, float* dst, size_t n
     if (!env || !dst) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
     Env& e = env->e;
     float* src = sky_ptr(e, param, dir);
+    if (!src && (param == SKT_DEBUG1 || param == SKT_DEBUG2))
+        return fail(&e, SKT_INVALID_ARG, "debug fields need skt_set_diagnostics(env, SKT_DIAG_BUOYANCY) first");
     if (!src) return fail(&e, SKT_INVALID_ARG, "unknown field selector");
     if (n != size_t(e.g.N)) return fail(&e, SKT_INVALID_ARG, "size mismatch");
     cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToHost, e.stream);

@@ -156,6 +156,13 @@ struct Env {
     void* mg_pool = nullptr;
     MgLevel mg[kMaxMgLevels];
     void* mg_h = nullptr;         // FP16 ax, ay, az, aw of the finest level (4 x N halves, in mg_pool)
+    // diagnostics (allocated when enabled, never during a step)
+    int rates_on = 0;
+    int rate_lo[3] = {0, 0, 0}, rate_hi[3] = {0, 0, 0};
+    double* rates_dev = nullptr;  // the 33 region-summed process amounts of the last step
+    int diag_flags = 0;
+    float* dbg_buoy = nullptr;    // buoyancy velocity change per cell (the second debug field)
+    float* dbg_zero = nullptr;    // the first debug field, which the step never writes
     // launch accounting and optional per-stage event timing
     long long launches = 0;
     float last_gpu_ms = 0.0f;

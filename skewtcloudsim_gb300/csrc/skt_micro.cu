@@ -8,16 +8,55 @@ namespace {
 
 constexpr int BX = 32, BY = 8;
 
+// the selection box of the region-summed process amounts (inclusive, reference layout x, y, z)
+struct RateBox {
+    int lo[3], hi[3];
+};
+constexpr int kRates = 33;
+
+// Region sums of the data graph (Game/microPhysics.cu:1356-1413): each block adds its cells'
+// 33 values (registers -> warp shuffles -> shared memory) and one thread per value adds the block
+// total to an FP64 accumulator; only blocks that meet the box take part.
+__device__ __forceinline__ void add_rates(const float (&v)[kRates], bool inside, bool block_meets, double* rates) {
+    if (!block_meets) return;
+    __shared__ float part[BX * BY / 32][kRates];
+    const int tid = threadIdx.x + BX * threadIdx.y, warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+    for (int k = 0; k < kRates; ++k) {
+        float a = inside ? v[k] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) part[warp][k] = a;
+    }
+    __syncthreads();
+    if (tid < kRates) {
+        double t = 0.0;
+        for (int w = 0; w < BX * BY / 32; ++w) t += double(part[w][tid]);
+        atomicAdd(rates + tid, t);
+    }
+}
+
 // calculateEnvMicroPhysicsGPU (Game/microPhysics.cu:1035-1354) + addHeatGPU
 // (Game/kernelSky.cu:1249-1282) in one pass: the condensation/deposition/freezing sums stay in
-// registers instead of three global arrays.
+// registers instead of three global arrays. RATES: also the region-summed process amounts.
+template <bool RATES>
 __global__ void __launch_bounds__(256) k_micro(Grid g, float* __restrict__ qv_, float* __restrict__ qw_, float* __restrict__ qc_,
                                                float* __restrict__ qr_, float* __restrict__ qs_, float* __restrict__ qi_,
                                                float* __restrict__ th, const float* __restrict__ rho, const float* __restrict__ p,
-                                               const float* __restrict__ Pg, float dt, float speed, Micro M) {
+                                               const float* __restrict__ Pg, float dt, float speed, Micro M, RateBox rb, double* rates) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
-    if (x >= g.X || y >= g.Y) return;
-    if (is_ground(g, x, y, z)) return;
+    bool live = x < g.X && y < g.Y && !is_ground(g, x, y, z);
+    if (!RATES && !live) return;
+    bool block_meets = false;
+    if (RATES) {
+        const int bx0 = blockIdx.x * BX, by0 = blockIdx.y * BY;
+        block_meets = bx0 <= rb.hi[0] && bx0 + BX - 1 >= rb.lo[0] && by0 <= rb.hi[1] && by0 + BY - 1 >= rb.lo[1] && z >= rb.lo[2] && z <= rb.hi[2];
+        if (!live) {
+            float zero[kRates] = {0};
+            add_rates(zero, false, block_meets, rates);
+            return;
+        }
+    }
     const int c = cidx(g, x, y, z);
     const float lo = 1e-18f;
     const float Qv = qv_[c] > lo ? qv_[c] : 0.0f, Qw = qw_[c] > lo ? qw_[c] : 0.0f;
@@ -139,6 +178,14 @@ __global__ void __launch_bounds__(256) k_micro(Grid g, float* __restrict__ qv_, 
         qi_[c] += -PGMLT + PGACS;
     }
     qv_[c] = nqv;
+    if (RATES) {
+        const bool inside = x >= rb.lo[0] && x <= rb.hi[0] && y >= rb.lo[1] && y <= rb.hi[1] && z >= rb.lo[2] && z <= rb.hi[2];
+        const float v[kRates] = {PVCON < 0.0f ? 0.0f : PVCON, PVDEP < 0.0f ? 0.0f : PVDEP, PIMLT, PIDW, PIHOM, PIACR, PRACI, PRAUT, PRACW,
+                                 PREVP, PRACS, PSACW, PSACR, PSACI, PSAUT, PSFW, PSFI, PSDEP, PSSUB, PSMLT, PGAUT, PGFR, PGACW, PGACI,
+                                 PGACR, PGDRY * (1 - WT), PGACS, PGSUB, PGMLT, PGWET * WT, PGACR1, PVCON < 0.0f ? -PVCON : 0.0f,
+                                 PVDEP < 0.0f ? -PVDEP : 0.0f};
+        add_rates(v, inside, block_meets, rates);
+    }
     // latent heat with the updated vapour (addHeatGPU)
     const float Mair = 0.02896f, Mwat = 0.01802f;
     const float XV = (nqv / Mwat) / ((nqv / Mwat) + (1 - nqv) / Mair);
@@ -372,8 +419,15 @@ void launch_micro(Env& e, float dt, float speed) {
     M.G = e.gam;
     ProfScope ps(e, "micro");
     e.launches += 1;
-    k_micro<<<dim3((g.X + BX - 1) / BX, (g.Y + BY - 1) / BY, g.Z), dim3(BX, BY), 0, e.stream>>>(g, e.qv, e.qw, e.qc, e.qr, e.qs, e.qi, e.th, e.rho,
-                                                                                          e.p, e.Pg, dt, speed, M);
+    const dim3 grid((g.X + BX - 1) / BX, (g.Y + BY - 1) / BY, g.Z), blk(BX, BY);
+    if (e.rates_on) {
+        RateBox rb{{e.rate_lo[0], e.rate_lo[1], e.rate_lo[2]}, {e.rate_hi[0], e.rate_hi[1], e.rate_hi[2]}};
+        cudaMemsetAsync(e.rates_dev, 0, sizeof(double) * kRates, e.stream);
+        k_micro<true><<<grid, blk, 0, e.stream>>>(g, e.qv, e.qw, e.qc, e.qr, e.qs, e.qi, e.th, e.rho, e.p, e.Pg, dt, speed, M, rb, e.rates_dev);
+    } else {
+        k_micro<false><<<grid, blk, 0, e.stream>>>(g, e.qv, e.qw, e.qc, e.qr, e.qs, e.qi, e.th, e.rho, e.p, e.Pg, dt, speed, M, RateBox{},
+                                                   nullptr);
+    }
 }
 
 void launch_ground(Env& e, float dt, float speed, float irr) {

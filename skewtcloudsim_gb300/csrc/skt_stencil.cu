@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(128) k_precip(Grid g, float* __restrict__ q, c
 __global__ void __launch_bounds__(256) k_buoyancy(Grid g, float* __restrict__ v, const float* __restrict__ th, const float* __restrict__ qv,
                                                   const float* __restrict__ qr, const float* __restrict__ qs, const float* __restrict__ qi,
                                                   const float* __restrict__ isenT, const float* __restrict__ isenQv,
-                                                  const float* __restrict__ p, const float* __restrict__ Pg, float dt) {
+                                                  const float* __restrict__ p, const float* __restrict__ Pg, float dt, float* __restrict__ dbg) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
     if (x >= g.X || y >= g.Y) return;
     if (is_ground(g, x, y, z)) return;
@@ -561,7 +561,10 @@ __global__ void __launch_bounds__(256) k_buoyancy(Grid g, float* __restrict__ v,
     const bool down = y > 0 && !is_ground(g, x, y - 1, z);
     auto valid = [&](int dx, int dz) { return in_dom(g, x + dx, y, z + dz) && !is_ground(g, x + dx, y, z + dz); };
     const int nv = int(valid(-1, 0)) + int(valid(1, 0)) + int(valid(0, -1)) + int(valid(0, 1));
-    if (nv == 0) return;
+    if (nv == 0) {
+        if (dbg) dbg[c] = 0.0f;
+        return;
+    }
     const float Pgs = Pg[x + z * g.X];
     const float psC = p[c];
     const float psU = up ? p[c + g.X] : psC;
@@ -610,6 +613,7 @@ __global__ void __launch_bounds__(256) k_buoyancy(Grid g, float* __restrict__ v,
     else if (vel < 0.0f) fin = BDown;
     float change = fin * dt;
     if ((up && vel > 0.0f && -change > vel) || (down && vel < 0.0f && -change < vel)) change = -vel;
+    if (dbg) dbg[c] = change;  // buoyancyStor, the reference's second debug field
     v[c] = vel + change;
 }
 
@@ -845,7 +849,8 @@ void launch_precip(Env& e, float* q, int type, float dtS) {
 void launch_buoyancy(Env& e, float dtS) {
     ProfScope ps(e, "buoyancy");
     e.launches += 1;
-    k_buoyancy<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.isenT, e.isenQv, e.p, e.Pg, dtS);
+    k_buoyancy<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.isenT, e.isenQv, e.p, e.Pg, dtS,
+                                                             (e.diag_flags & SKT_DIAG_BUOYANCY) ? e.dbg_buoy : nullptr);
 }
 void launch_init_density(Env& e) {
     ProfScope ps(e, "eos");

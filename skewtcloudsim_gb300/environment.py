@@ -42,6 +42,9 @@ class Parameter(IntEnum):  # Game/config.h:62-65
     WIND = 7
     PGROUND = 8
     PRESSURE = 9
+    DEBUG1 = 10
+    DEBUG2 = 11
+    DEBUG3 = 12
     DENSITY = 100
 
 
@@ -84,7 +87,15 @@ FIELDS = {
     "qr": (Parameter.QR, 0), "qs": (Parameter.QS, 0), "qi": (Parameter.QI, 0),
     "u": (Parameter.WIND, Direction.RIGHT), "v": (Parameter.WIND, Direction.UP), "w": (Parameter.WIND, Direction.FORWARD),
     "p": (Parameter.PRESSURE, 0), "rho": (Parameter.DENSITY, 0),
+    # the reference's editor debug views: DEBUG1 never written (zeros), DEBUG2 the buoyancy velocity
+    # change (needs set_diagnostics(DIAG_BUOYANCY)), DEBUG3 the projection's pressure correction
+    "debug1": (Parameter.DEBUG1, 0), "debug2": (Parameter.DEBUG2, 0), "debug3": (Parameter.DEBUG3, 0),
 }
+DIAG_BUOYANCY = 1
+# the 33 region-summed microphysics amounts (microPhysicsParams order, Game/microPhysics.cuh:7-21)
+RATE_NAMES = ("PVCON", "PVDEP", "PIMLT", "PIDW", "PIHOM", "PIACR", "PRACI", "PRAUT", "PRACW", "PREVP", "PRACS", "PSACW",
+              "PSACR", "PSACI", "PSAUT", "PSFW", "PSFI", "PSDEP", "PSSUB", "PSMLT", "PGAUT", "PGFR", "PGACW", "PGACI",
+              "PGACR", "PGDRY", "PGACS", "PGSUB", "PGMLT", "PGWET", "PGACR1", "PVVAP", "PVSUB")
 GROUND_FIELDS = {"Qrs": Ground.QRS, "Qgr": Ground.QGR, "Qgs": Ground.QGS, "Qgi": Ground.QGI, "Pg": Ground.P,
                  "tg": Ground.TIME_WET, "Tg": Ground.T, "cover": Ground.CLOUD_COVER}
 COLUMNS = {"isenT": Column.ISEN_T, "isenQv": Column.ISEN_QV, "defU": Column.DEF_U, "defW": Column.DEF_W}
@@ -209,6 +220,22 @@ class Environment:
             self._check(self._L.skt_write_column(self._h, int(COLUMNS[name]), _fp(a), a.size))
         else:
             raise KeyError(name)
+
+    # -- diagnostics (the reference's data graph and debug views) ----------------------------
+    def set_rate_region(self, lo=None, hi=None, enable: bool = True):
+        """Sum the microphysics process amounts over lo <= (x, y, z) <= hi (reference layout, y
+        vertical, inclusive) every step; enable=False turns it off."""
+        lo3 = (ctypes.c_int * 3)(*(lo or (0, 0, 0)))
+        hi3 = (ctypes.c_int * 3)(*(hi or (self.nx - 1, self.ny - 1, self.nz - 1)))
+        self._check(self._L.skt_set_rate_region(self._h, 1 if enable else 0, lo3, hi3))
+
+    def read_rates(self) -> dict:
+        out = np.empty(len(RATE_NAMES), np.float32)
+        self._check(self._L.skt_read_rates(self._h, _fp(out), out.size))
+        return dict(zip(RATE_NAMES, out.tolist()))
+
+    def set_diagnostics(self, flags: int):
+        self._check(self._L.skt_set_diagnostics(self._h, int(flags)))
 
     def set_clock(self, sim_time=43200.0, day=130, longitude=52.37, sun=1.0, pause=0):
         self._check(self._L.skt_set_clock(self._h, sim_time, day, longitude, sun, pause))
