@@ -204,6 +204,36 @@ skt_status skt_read_rates(skt_env* env, float* host_dst, size_t n);
 #define SKT_DIAG_BUOYANCY 1
 skt_status skt_set_diagnostics(skt_env* env, int flags);
 
+/* ---- Editing between steps (the reference's editor tools) -------------------------------- */
+
+/* Replaces environmentGPU::prepareBrushGPU (Game/environment.cu:1127-1186, kernel applyBrushGPU
+ * Game/kernelSky.cu:1476-1549). param: SKT_POTTEMP, SKT_QV..SKT_QI, SKT_WIND (the amount split by
+ * dir[3] into u, v, w) or SKT_PGROUND (raise the heightfield to the brushed cells, or with
+ * ground_erase lower it to the lowest brushed ground cell; cells an erase frees take the default
+ * columns). Adds (1 - d^2/r^2)^smoothness * dt * intensity * value to the sky cells at squared
+ * distance d^2 <= r^2 = brush_size^2 from pos (reference layout x, y vertical, z); the brush box
+ * reaches -ceil(r) .. ceil(r)-1 in x and y, as the reference's. *ground_changed (optional) tells
+ * whether the heightfield changed. SKT_PRESSURE is rejected (the reference has no pressure array
+ * for it). Synchronous. */
+skt_status skt_apply_brush(skt_env* env, int param, float brush_size, const int pos[3], float smoothness, float dt, float intensity,
+                           float value, const float dir[3], int ground_erase, int* ground_changed);
+
+/* Replaces environmentGPU::prepareSelectionGPU (Game/environment.cu:1188-1262, kernel
+ * applySelectionGPU Game/kernelSky.cu:1551-1595): sets value (wind: split by dir) on the sky cells
+ * of the box lo..hi (inclusive; an empty x or y extent becomes one cell, as the reference's host
+ * code does), or edits the heightfield as skt_apply_brush. Synchronous. */
+skt_status skt_apply_selection(skt_env* env, int param, const int lo[3], const int hi[3], float value, const float dir[3], int ground_erase,
+                               int* ground_changed);
+
+/* Replaces environmentGPU::resetParameterGPU (Game/environment.cu:1264-1285): theta, Qv, wind
+ * (u, w) and pressure back to their default columns (each (x, y) column of cells stops at its
+ * first ground cell, as the reference's setToDefault does), v and Qw..Qi to 0 everywhere.
+ * Synchronous. */
+skt_status skt_reset_parameter(skt_env* env, int param);
+
+/* The current heightfield (nx*nz values). Synchronous. */
+skt_status skt_read_ground_height(skt_env* env, int32_t* host_dst, size_t n);
+
 /* Text of the last error on env (or, when env is NULL, of the last skt_create or
  * skt_diffuse_noalloc failure on this thread). */
 const char* skt_last_error(const skt_env* env);

@@ -81,6 +81,17 @@ def lib():
         L.oc_buoyancy_dbg_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_float,
                                           ctypes.POINTER(ctypes.c_float)]
         L.oc_buoyancy_dbg_f32.restype = ctypes.c_int
+        FP, IP = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
+        L.oc_brush_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_int, ctypes.c_float, IP,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, FP, ctypes.c_int, FP]
+        L.oc_brush_f32.restype = ctypes.c_int
+        L.oc_selection_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_int, IP, IP,
+                                       ctypes.c_float, FP, ctypes.c_int, FP]
+        L.oc_selection_f32.restype = ctypes.c_int
+        L.oc_reset_parameter_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState), ctypes.c_int, FP]
+        L.oc_reset_parameter_f32.restype = ctypes.c_int
+        L.oc_editor_block_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState)]
+        L.oc_editor_block_f32.restype = ctypes.c_int
         L.oc_irradiance.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
         L.oc_irradiance.restype = ctypes.c_float
         L.oc_num_threads.restype = ctypes.c_int
@@ -132,6 +143,9 @@ class OracleState:
         self.gh = np.ascontiguousarray(init.ground_height, np.int32).copy()
         self.sim_time = 43200.0
         self.day, self.longitude, self.sun, self.pause = 130, 52.37, 1.0, 0
+        # the reference's m_groundChanged after the init pass: set by ground edits, it runs
+        # editorDataGPU's ground block after the edit and at the start of the next step
+        self.ground_changed = False
         st = self._cstate()
         fn = lib().oc_init_f32 if self.dtype == np.float32 else lib().oc_init_f64
         fn(self.X, self.Y, self.Z, ctypes.byref(st), int(noise))
@@ -144,7 +158,14 @@ class OracleState:
         st.sim_time, st.day, st.longitude, st.sun, st.pause = self.sim_time, self.day, self.longitude, self.sun, self.pause
         return st
 
+    def _editor_block(self):
+        assert self.dtype == np.float32
+        st = self._cstate()
+        lib().oc_editor_block_f32(self.X, self.Y, self.Z, ctypes.byref(st))
+
     def step(self, cfg: Config, dt: float, speed: float = 1.0):
+        if self.ground_changed:
+            self._editor_block()
         st = self._cstate()
         d = OcDiag()
         fn = lib().oc_step_f32 if self.dtype == np.float32 else lib().oc_step_f64
@@ -153,6 +174,7 @@ class OracleState:
         if rc != 0:
             raise RuntimeError(f"oracle step failed: {rc}")
         self.sim_time = st.sim_time
+        self.ground_changed = False
         return {"pcg_iters": d.pcg_iters, "pcg_residual": d.pcg_residual, "nsub": list(d.nsub),
                 "converged": bool(d.converged)}
 
@@ -183,6 +205,38 @@ class OracleState:
         st = self._cstate()
         lib().oc_buoyancy_dbg_f32(self.X, self.Y, self.Z, ctypes.byref(st), dt, dbg.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
         return dbg
+
+    # -- editing (prepareBrushGPU / prepareSelectionGPU / resetParameterGPU) --------------------
+    def brush(self, param, size, pos, smooth, dt, intensity, value, direction=(1.0, 0.0, 0.0), erase=False, p_column=None):
+        st = self._cstate()
+        pc = np.ascontiguousarray(p_column, np.float32)
+        r = lib().oc_brush_f32(self.X, self.Y, self.Z, ctypes.byref(st), int(param), size, (ctypes.c_int * 3)(*pos), smooth, dt,
+                               intensity, value, (ctypes.c_float * 3)(*direction), int(erase),
+                               pc.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        if r < 0:
+            raise ValueError("bad parameter")
+        self.ground_changed |= bool(r)
+        if self.ground_changed:
+            self._editor_block()
+        return bool(r)
+
+    def selection(self, param, lo, hi, value, direction=(1.0, 0.0, 0.0), erase=False, p_column=None):
+        st = self._cstate()
+        pc = np.ascontiguousarray(p_column, np.float32)
+        r = lib().oc_selection_f32(self.X, self.Y, self.Z, ctypes.byref(st), int(param), (ctypes.c_int * 3)(*lo),
+                                   (ctypes.c_int * 3)(*hi), value, (ctypes.c_float * 3)(*direction), int(erase),
+                                   pc.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        if r < 0:
+            raise ValueError("bad parameter")
+        self.ground_changed |= bool(r)
+        if self.ground_changed:
+            self._editor_block()
+        return bool(r)
+
+    def reset_parameter(self, param, p_column=None):
+        st = self._cstate()
+        pc = np.ascontiguousarray(p_column, np.float32)
+        lib().oc_reset_parameter_f32(self.X, self.Y, self.Z, ctypes.byref(st), int(param), pc.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
 
     def sky_mask(self):
         y = np.arange(self.Y)[None, :, None]

@@ -1082,6 +1082,164 @@ template <class T> void init_state(int X, int Y, int Z, State<T>& s, int noise) 
         }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Editing: prepareBrushGPU / prepareSelectionGPU / resetParameterGPU (Game/environment.cu:1127-1290)
+// with applyBrushGPU, applySelectionGPU, setGround, compareAndResetValuesOutGround
+// (Game/kernelSky.cu:1476-1642), editorDataGPU's ground block (Game/environment.cu:989-1011),
+// setToDefault / setToValue (Game/kernelSky.cu:1714-1728, Game/kernelMaths.cu:12-23).
+// Parameters: 0 theta, 1 Qv .. 6 Qi, 7 wind, 8 ground (Game/config.h:62-65).
+// Two differences: the reference's bounds test lets z = Z through (`mZ > GRIDSIZESKYZ`) and writes
+// one plane past the field, here that plane is skipped; a raise stops at row Y-2 so that every
+// column keeps a sky cell.
+// ---------------------------------------------------------------------------------------------
+struct EditParams {
+    int param;
+    float value, dir[3];
+    int erase;
+};
+
+template <class T> T* edit_field(State<T>& s, int param) {
+    T* f[7] = {s.th, s.qv, s.qw, s.qc, s.qr, s.qs, s.qi};
+    return param >= 0 && param < 7 ? f[param] : nullptr;
+}
+
+// one brushed/selected cell; amount = the value before the wind split. Returns true when the
+// ground store changed (setGround, Game/kernelSky.cu:1597-1611).
+template <class T>
+bool edit_cell(const Grid& g, State<T>& s, std::vector<int32_t>& ghn, const EditParams& ep, int x, int y, int z, float amount, bool add) {
+    const int ig = x + z * g.X;
+    if (ep.param == 8) {
+        if (ep.erase && y <= g.gh[ig]) { ghn[ig] = std::min(ghn[ig], y); return true; }
+        if (!ep.erase && y > g.gh[ig]) { ghn[ig] = std::max(ghn[ig], std::min(y, g.Y - 2)); return true; }  // keep a sky cell
+        return false;
+    }
+    const int64_t idx = g.id(x, y, z);
+    float v1 = amount, v2 = 0, v3 = 0;
+    if (ep.param == 7) {
+        v3 = v1 * ep.dir[2];
+        v2 = v1 * ep.dir[1];
+        v1 *= ep.dir[0];
+        if (add) { s.u[idx] += v1; s.v[idx] += v2; s.w[idx] += v3; }
+        else { s.u[idx] = v1; s.v[idx] = v2; s.w[idx] = v3; }
+    } else {
+        T* f = edit_field(s, ep.param);
+        if (add) f[idx] += v1;
+        else f[idx] = v1;
+    }
+    return false;
+}
+
+// editorDataGPU's block (Game/environment.cu:992-1011), run after an edit and at the start of the
+// next step while the ground has changed: ground cells of theta, Qv, Qw..Qi, u, v to 0; the ground
+// temperature from the isentrope (computeIsenTempGroundGPU Game/kernelGround.cu:38-47)
+template <class T> void editor_block(const Grid& g, State<T>& s) {
+    const int X = g.X, Y = g.Y, Z = g.Z;
+    T* fl[9] = {s.th, s.qv, s.qw, s.qc, s.qr, s.qs, s.qi, s.u, s.v};
+    for (int z = 0; z < Z; ++z)
+        for (int y = 0; y < Y; ++y)
+            for (int x = 0; x < X; ++x)
+                if (g.ground(x, y, z))
+                    for (T* f : fl) f[g.id(x, y, z)] = 0;
+    for (int z = 0; z < Z; ++z)
+        for (int x = 0; x < X; ++x) {
+            const int idx = x + z * X;
+            const int GH = s.gh[idx] + 1 >= Y ? Y - 1 : s.gh[idx] + 1;
+            const T Tt = potentialTemp(s.isenT[GH - 1] - T(273.15), s.Pg[idx], s.p[g.id(x, GH, z)]);
+            s.Tg[idx] = Tt + T(273.15);
+        }
+}
+
+// after an edit whose ground store changed: reset the cells an erase freed, take the new heights
+template <class T> void edit_finish(Grid& g, State<T>& s, std::vector<int32_t>& ghn, bool erase, const T* pcol) {
+    const int X = g.X, Y = g.Y, Z = g.Z;
+    if (erase)
+        for (int z = 0; z < Z; ++z)
+            for (int y = 0; y < Y; ++y)
+                for (int x = 0; x < X; ++x) {
+                    const int ig = x + z * X;
+                    if (y > s.gh[ig] || y <= ghn[ig]) continue;
+                    const int64_t idx = g.id(x, y, z);
+                    s.qv[idx] = s.isenQv[y];
+                    s.qw[idx] = s.qc[idx] = s.qr[idx] = s.qs[idx] = s.qi[idx] = 0;
+                    s.th[idx] = s.isenT[y];
+                    s.u[idx] = s.v[idx] = s.w[idx] = 0;
+                    s.p[idx] = pcol[y];
+                }
+    std::copy(ghn.begin(), ghn.end(), s.gh);
+}
+
+// applyBrushGPU: the brush box is ceil(r) - floor(-r) cells wide in x and y, offset by ceil(r)
+// (so x and y reach -ceil(r) .. ceil(r)-1), and runs over the whole column range in z
+template <class T>
+int brush(Grid& g, State<T>& s, const EditParams& ep, float size, const int pos[3], float smooth, float dt, float intensity, const T* pcol) {
+    const int c = int(std::ceil(size));
+    const int n = int(std::ceil(size)) - int(std::floor(-size));
+    std::vector<int32_t> ghn(s.gh, s.gh + size_t(g.X) * g.Z);
+    bool changed = false;
+    for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x)
+            for (int z = 0; z < g.Z; ++z) {
+                const int lX = x - c, lY = y - c, lZ = z - c;
+                const int mX = x + pos[0] - c, mY = y + pos[1] - c, mZ = z + pos[2] - c;
+                if (mX >= g.X || mY >= g.Y || mZ >= g.Z || mX < 0 || mY < 0 || mZ < 0) continue;
+                if (ep.param != 8 && mY <= g.gh[mX + mZ * g.X]) continue;
+                const float d = float(lX) * float(lX) + float(lY) * float(lY) + float(lZ) * float(lZ);
+                const float r = size * size;
+                if (!(d <= r)) continue;
+                float v = -(d / r - 1);
+                v = std::pow(v, smooth);
+                v *= dt * intensity * ep.value;
+                changed |= edit_cell(g, s, ghn, ep, mX, mY, mZ, v, true);
+            }
+    if (changed) edit_finish(g, s, ghn, ep.erase != 0, pcol);
+    return changed ? 1 : 0;
+}
+
+// applySelectionGPU: the box lo..hi (an empty x or y extent becomes one cell, as the host code does)
+template <class T> int selection(Grid& g, State<T>& s, const EditParams& ep, const int lo[3], const int hi[3], const T* pcol) {
+    int ny = hi[1] - lo[1] + 1, nx = hi[0] - lo[0] + 1;
+    if (ny <= 0) ny = 1;
+    if (nx <= 0) nx = 1;
+    std::vector<int32_t> ghn(s.gh, s.gh + size_t(g.X) * g.Z);
+    bool changed = false;
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x)
+            for (int z = lo[2]; z <= hi[2]; ++z) {
+                const int mX = x + lo[0], mY = y + lo[1], mZ = z;
+                if (mX >= g.X || mY >= g.Y || mZ >= g.Z || mX < 0 || mY < 0 || mZ < 0) continue;
+                if (ep.param != 8 && mY <= g.gh[mX + mZ * g.X]) continue;
+                changed |= edit_cell(g, s, ghn, ep, mX, mY, mZ, ep.value, false);
+            }
+    if (changed) edit_finish(g, s, ghn, ep.erase != 0, pcol);
+    return changed ? 1 : 0;
+}
+
+// resetParameterGPU: setToDefault stops each (x, y) column at its first ground cell in z;
+// setToValue covers every cell
+template <class T> void reset_parameter(const Grid& g, State<T>& s, int param, const T* pcol) {
+    auto to_default = [&](T* f, const T* def) {
+        for (int y = 0; y < g.Y; ++y)
+            for (int x = 0; x < g.X; ++x)
+                for (int z = 0; z < g.Z; ++z) {
+                    if (g.ground(x, y, z)) break;
+                    f[g.id(x, y, z)] = def[y];
+                }
+    };
+    auto to_value = [&](T* f, T v) { std::fill(f, f + g.n(), v); };
+    switch (param) {
+        case 0: to_default(s.th, s.isenT); break;
+        case 7: to_default(s.u, s.defU); to_value(s.v, T(0)); to_default(s.w, s.defW); break;
+        case 9: to_default(s.p, pcol); break;
+        case 1: to_default(s.qv, s.isenQv); break;
+        case 2: to_value(s.qw, T(0)); break;
+        case 3: to_value(s.qc, T(0)); break;
+        case 4: to_value(s.qr, T(0)); break;
+        case 5: to_value(s.qs, T(0)); break;
+        case 6: to_value(s.qi, T(0)); break;
+        default: break;
+    }
+}
+
 }  // namespace skt_oracle
 
 // ------------------------------------- C ABI for the tests --------------------------------------
@@ -1223,6 +1381,39 @@ int oc_micro_rates_f32(int X, int Y, int Z, oc_state* st, float dt, float speed,
     RateRegion rr{{region[0], region[1], region[2]}, {region[3], region[4], region[5]}, {0}};
     microphysics_sky(g, s, dt, speed, M, &rr);
     for (int k = 0; k < 33; ++k) out[k] = rr.sums[k];
+    return 0;
+}
+
+// editing (f32 state): returns 1 when the ground changed, 0 otherwise, -1 for a bad parameter
+int oc_brush_f32(int X, int Y, int Z, oc_state* st, int param, float size, const int* pos, float smooth, float dt, float intensity,
+                 float value, const float* dir, int erase, const float* pcol) {
+    if (param < 0 || param > 8) return -1;
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    EditParams ep{param, value, {dir[0], dir[1], dir[2]}, erase};
+    return brush(g, s, ep, size, pos, smooth, dt, intensity, pcol);
+}
+
+int oc_selection_f32(int X, int Y, int Z, oc_state* st, int param, const int* lo, const int* hi, float value, const float* dir, int erase,
+                     const float* pcol) {
+    if (param < 0 || param > 8) return -1;
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    EditParams ep{param, value, {dir[0], dir[1], dir[2]}, erase};
+    return selection(g, s, ep, lo, hi, pcol);
+}
+
+int oc_editor_block_f32(int X, int Y, int Z, oc_state* st) {
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    editor_block(g, s);
+    return 0;
+}
+
+int oc_reset_parameter_f32(int X, int Y, int Z, oc_state* st, int param, const float* pcol) {
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    reset_parameter(g, s, param, pcol);
     return 0;
 }
 

@@ -61,6 +61,13 @@ SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_int)]),
     "skt_read_rates": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_size_t]),
     "skt_set_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "skt_apply_brush": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.POINTER(ctypes.c_int), ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_float, ctypes.c_float, c_float_p, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int)]),
+    "skt_apply_selection": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                           ctypes.c_float, c_float_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "skt_reset_parameter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "skt_read_ground_height": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_size_t]),
     "skt_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "skt_version": (ctypes.c_char_p, []),
 }

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libskewt_gb300.so")
 ROOT = os.path.dirname(HERE)
 
-SOURCES = ["skt_api.cu", "skt_stencil.cu", "skt_project.cu", "skt_micro.cu", "skt_mg.cu"]
+SOURCES = ["skt_api.cu", "skt_stencil.cu", "skt_project.cu", "skt_micro.cu", "skt_mg.cu", "skt_edit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -12,10 +12,6 @@
 
 using namespace skt;
 
-struct skt_env {
-    Env e;
-};
-
 namespace {
 
 thread_local std::string g_create_err;
@@ -102,6 +98,8 @@ skt_status run_step(Env& e, float dt, float speed) {
     const float dtS = dt * speed;
     const bool hs = true;
     const float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
+    // editorDataGPU at the start of updateGPU (Game/environment.cu:398): after a ground edit
+    if (e.ground_changed) launch_editor_block(e);
     // ground, then setTempsAtGround (fused into the ground column kernel)
     launch_ground(e, dt, speed, irr);
     // theta
@@ -146,6 +144,8 @@ skt_status run_step(Env& e, float dt, float speed) {
 
 namespace skt {
 void set_global_error(const char* msg) { g_create_err = msg ? msg : ""; }
+skt_status report(Env* e, skt_status st, const char* msg) { return fail(e, st, msg); }
+skt_status check_cuda(Env& e, const char* where) { return cuda_check(e, where); }
 }  // namespace skt
 
 extern "C" {
@@ -252,7 +252,7 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     const size_t N = size_t(n), NG = size_t(grid->nx) * grid->nz, NY = size_t(grid->ny);
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const int nsky = 12 + 2 + 4 + 4;
-    size_t bytes = al(N * 4) * nsky + al(N * 8) * 2 + al(NG * 4) * 10 + al(NG * 4) + al(NY * 4) * 5 + al(sizeof(Scalars)) +
+    size_t bytes = al(N * 4) * nsky + al(N * 8) * 2 + al(NG * 4) * 10 + al(NG * 4) + al(NY * 4) * 6 + al(sizeof(Scalars)) +
                    al(sizeof(double) * 2 * kMaxPartials);
     if (cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking) != cudaSuccess) {
         const std::string m = std::string("stream: ") + cudaGetErrorString(cudaGetLastError());
@@ -276,8 +276,8 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     float** gr[10] = {&e.Qrs, &e.Qgr, &e.Qgs, &e.Qgi, &e.Pg, &e.tg, &e.Tg, &e.cover, &e.g2a, &e.g2b};
     for (int i = 0; i < 10; ++i) *gr[i] = (float*)take(NG * 4);
     e.gh = (int*)take(NG * 4);
-    float** co[5] = {&e.isenT, &e.isenQv, &e.defU, &e.defW, &e.zeroY};
-    for (int i = 0; i < 5; ++i) *co[i] = (float*)take(NY * 4);
+    float** co[6] = {&e.isenT, &e.isenQv, &e.defU, &e.defW, &e.zeroY, &e.pcol};
+    for (int i = 0; i < 6; ++i) *co[i] = (float*)take(NY * 4);
     e.sc = (Scalars*)take(sizeof(Scalars));
     e.partials = (double*)take(sizeof(double) * 2 * kMaxPartials);
     cudaMemsetAsync(e.pool, 0, bytes, e.stream);
@@ -347,7 +347,7 @@ skt_status skt_init(skt_env* env, const float* theta, const float* vel, const fl
     if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
     Env& e = env->e;
     if (!theta || !vel || !qv || !ground_T || !ground_p || !p3d || !gh) return fail(&e, SKT_INVALID_ARG, "null input array");
-    (void)p_column;  // the reference stores it for the editor only (m_defaultPressure)
+    // the reference keeps the pressure column for the editor's resets (m_defaultPressure)
     const size_t N = size_t(e.g.N), NG = size_t(e.g.X) * e.g.Z;
     for (size_t i = 0; i < NG; ++i)
         if (gh[i] < 0 || gh[i] >= e.g.Y - 1)
@@ -371,6 +371,9 @@ skt_status skt_init(skt_env* env, const float* theta, const float* vel, const fl
     cudaMemcpyAsync(e.Pg, ground_p, NG * 4, cudaMemcpyHostToDevice, e.stream);
     cudaMemcpyAsync(e.p, p3d, N * 4, cudaMemcpyHostToDevice, e.stream);
     cudaMemcpyAsync(e.gh, gh, NG * 4, cudaMemcpyHostToDevice, e.stream);
+    if (p_column) cudaMemcpyAsync(e.pcol, p_column, size_t(e.g.Y) * 4, cudaMemcpyHostToDevice, e.stream);
+    else cudaMemsetAsync(e.pcol, 0, size_t(e.g.Y) * 4, e.stream);
+    e.ground_changed = 0;  // the init does the first editorDataGPU pass itself
     launch_init_state(e, (flags & SKT_INIT_NOISE) ? 1 : 0, noise_seed);
     cudaStreamSynchronize(e.stream);
     const skt_status st = cuda_check(e, "init");
@@ -389,6 +392,7 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     for (int i = 0; i < nsteps; ++i) {
         const skt_status st = run_step(e, dt, speed);
         if (st != SKT_OK) return st;
+        e.ground_changed = 0;  // Game/environment.cu:554
         if (!e.last_converged) worst = SKT_NOT_CONVERGED;
     }
     cudaEventRecord(e.ev1, e.stream);

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "skt_physics.cuh"
+#include "../../include/skewt.h"
 
 namespace skt {
 
@@ -81,6 +82,7 @@ struct Scalars {
     float inner_tol;                  // mixed mode: max residual at the start of the inner solve
     int outer_inner_total;            // mixed mode: inner iterations summed over the refinement
     int refine_done;                  // mixed mode: relative FP64 residual met refine_tol
+    int edit_changed;                 // an edit changed the ground store
 };
 
 // one coarse level of the multigrid preconditioner (A-form coefficients and work vectors)
@@ -126,6 +128,8 @@ struct Env {
     int* gh;
     // columns (Y)
     float *isenT, *isenQv, *defU, *defW, *zeroY;
+    float* pcol = nullptr;        // the init's pressure column (the editor's pressure reset)
+    int ground_changed = 0;       // the ground changed since the last step (m_groundChanged)
     // reductions
     Scalars* sc;
     double* partials;
@@ -202,8 +206,20 @@ void launch_project(Env& e, float dtS);
 void launch_micro(Env& e, float dt, float speed);
 void launch_ground(Env& e, float dt, float speed, float irr);
 void launch_init_state(Env& e, int noise, uint32_t seed);
+void launch_isen_ground(Env& e);  // computeIsenTempGroundGPU on the current heightfield
+void launch_editor_block(Env& e);  // editorDataGPU's ground block (after a ground edit)
 bool mg_allocate(Env& e);
 void launch_matvec_textbook(Env& e, const float* s, float* As);
 void mg_solve(Env& e);
 
+// C-ABI helpers of skt_api.cu: record the error text on e (or, for e == nullptr, the thread's
+// create error) and return st; turn a pending CUDA error into a status
+skt_status report(Env* e, skt_status st, const char* msg);
+skt_status check_cuda(Env& e, const char* where);
+
 }  // namespace skt
+
+// the opaque handle of include/skewt.h
+struct skt_env {
+    skt::Env e;
+};

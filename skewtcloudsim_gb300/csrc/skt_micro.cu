@@ -444,6 +444,12 @@ void launch_ground(Env& e, float dt, float speed, float irr) {
     k_ground_column<<<(n2 + 127) / 128, 128, 0, e.stream>>>(g, P, dt, speed, irr, M);
 }
 
+void launch_isen_ground(Env& e) {
+    const Grid& g = e.g;
+    k_isen_ground<<<(g.X * g.Z + 127) / 128, 128, 0, e.stream>>>(g, e.Tg, e.isenT, e.Pg, e.p);
+    e.launches += 1;
+}
+
 void launch_init_state(Env& e, int noise, uint32_t seed) {
     const Grid& g = e.g;
     launch_init_density(e);

@@ -268,4 +268,27 @@ class Environment:
         return (y > gh.reshape(self.nz, self.nx)[:, None, :]).reshape(-1)
 
     def read_ground_height(self):
-        return np.zeros(self.ng, np.int32) if getattr(self, "_gh", None) is None else self._gh
+        out = np.empty(self.ng, np.int32)
+        self._check(self._L.skt_read_ground_height(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), out.size))
+        return out
+
+    # -- editing between steps (the reference's editor tools) -------------------------------
+    def apply_brush(self, param, size, pos, smoothness, dt, intensity, value, direction=(1.0, 0.0, 0.0), erase=False) -> bool:
+        """prepareBrushGPU: returns whether the heightfield changed."""
+        ch = ctypes.c_int(0)
+        d = np.asarray(direction, np.float32)
+        self._check(self._L.skt_apply_brush(self._h, int(param), size, (ctypes.c_int * 3)(*pos), smoothness, dt, intensity, value,
+                                            _fp(d), int(erase), ctypes.byref(ch)))
+        return bool(ch.value)
+
+    def apply_selection(self, param, lo, hi, value, direction=(1.0, 0.0, 0.0), erase=False) -> bool:
+        """prepareSelectionGPU: returns whether the heightfield changed."""
+        ch = ctypes.c_int(0)
+        d = np.asarray(direction, np.float32)
+        self._check(self._L.skt_apply_selection(self._h, int(param), (ctypes.c_int * 3)(*lo), (ctypes.c_int * 3)(*hi), value, _fp(d),
+                                                int(erase), ctypes.byref(ch)))
+        return bool(ch.value)
+
+    def reset_parameter(self, param):
+        """resetParameterGPU."""
+        self._check(self._L.skt_reset_parameter(self._h, int(param)))
