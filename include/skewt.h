@@ -234,8 +234,64 @@ skt_status skt_reset_parameter(skt_env* env, int param);
 /* The current heightfield (nx*nz values). Synchronous. */
 skt_status skt_read_ground_height(skt_env* env, int32_t* host_dst, size_t n);
 
-/* Text of the last error on env (or, when env is NULL, of the last skt_create or
- * skt_diffuse_noalloc failure on this thread). */
+/* ---- Sounding ingestion: the radiosonde readers and column interpolation of readTable ---- */
+
+/* One radiosonde ascent, radioSondeData (Game/readTable.h:9-47): n rows in file order (bottom
+ * up). Arrays filled by skt_sounding_read_* belong to the library (skt_sounding_free); a caller
+ * may also point them at its own arrays to feed skt_sounding_to_init. */
+typedef struct {
+    size_t n;
+    float* altitude;    /* m above sea level */
+    float* pressure;    /* hPa */
+    float* temperature; /* deg C */
+    float* dew_point;   /* deg C */
+    float* wind_speed;  /* m/s */
+    float* wind_dir;    /* degrees (the direction the wind blows from) */
+} skt_sounding;
+
+/* Archive access: the two calls readTable makes on its zip archive (miniz_cpp::zip_file::has_file
+ * and read, Game/zip_file.hpp:5286,5459). Returns the size in bytes of the member `name`, or -1
+ * when the archive has no such member; when buf is not NULL and cap is at least that size, the
+ * member's bytes are copied to buf first. */
+typedef long long (*skt_archive_read_fn)(void* ctx, const char* name, char* buf, size_t cap);
+
+/* Replaces readTable::readKNMIFile (Game/readTable.cpp:27-132): parses the member
+ * SynchronizedSoundingData.xml of a KNMI .mwx archive. As there: the first line is skipped; on
+ * every later line the whitespace-separated tokens 4..8 are pressure (hPa), temperature (K),
+ * relative humidity (%), wind direction and wind speed, each read after a fixed-length
+ * attribute prefix (10, 13, 10, 9, 11 characters) with its closing quote dropped, and any other
+ * token that starts with "Altitude" is the altitude; the dew point is
+ * T - (100 - RH) * 0.2 * (T + 273.15) * 0.01 (deg C); the last line read is not a row.
+ * Where the reference's reads would go out of bounds (short tokens, missing columns) or std::stof
+ * would throw, this returns SKT_INVALID_ARG. On error *out is left empty. */
+skt_status skt_sounding_read_knmi(skt_archive_read_fn read, void* ctx, skt_sounding* out);
+
+/* Replaces readTable::readDWDFile (Game/readTable.cpp:134-354) for a DWD "sekundenwerte aero"
+ * archive. archive_name is the string the reference splits on '_' for the station number (its
+ * third field). As there: the member Metadaten_Sekunde_Aero_<station>.txt lists the ascents
+ * (field 1 less its two last characters is a date); the ascent read is the one of date 161 at
+ * 12 UTC, from the member produkt_sec_aero_<first date>_<last date>_<station>.txt, found with the
+ * reference's search (100000-byte forward probes, then a scan from 100000 bytes back), which
+ * decides which rows are read: it can miss the first rows of an ascent or an ascent near the
+ * end of the member. Fields 6, 7, 8, 10, 11, 12 are altitude, pressure, temperature, dew point,
+ * wind speed and direction. Returns SKT_INVALID_ARG where the reference prints an error and
+ * reads nothing (missing member, date not found) and where it would read out of bounds. */
+skt_status skt_sounding_read_dwd(const char* archive_name, skt_archive_read_fn read, void* ctx, skt_sounding* out);
+
+/* Frees the arrays of a sounding filled by skt_sounding_read_*; leaves it empty. */
+void skt_sounding_free(skt_sounding* s);
+
+/* Replaces readTable::initEnvironment (Game/readTable.cpp:364-474) for a run-time grid: the
+ * arrays skt_init takes, every column a copy of the sounding interpolated to the level heights
+ * y*voxel above the first row (theta relative to the first row's pressure, Qv = ws(dew point,
+ * p), wind from direction and speed on MAC faces, ground T and p from the first row). The
+ * outputs are nx*ny*nz (vel_aos3 three times that), nx*nz (ground) and ny (p_column) floats.
+ * SKT_INVALID_ARG when the sounding ends below the grid top. */
+skt_status skt_sounding_to_init(const skt_sounding* s, const skt_grid_desc* grid, float* theta, float* vel_aos3,
+                                float* qv, float* ground_T, float* ground_p, float* p3d, float* p_column);
+
+/* Text of the last error on env (or, when env is NULL, of the last skt_create,
+ * skt_diffuse_noalloc or skt_sounding_* failure on this thread). */
 const char* skt_last_error(const skt_env* env);
 
 /* Library version string. */

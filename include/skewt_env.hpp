@@ -7,6 +7,8 @@
 //   Game.EnvGPU().updateGPU(dt, speed)  (Game/game.cpp:56) -> env.updateGPU(dt, speed)
 //   getParamArray(parameter, direction) (Game/environment.cu:1076) -> env.getParamArray(...)
 //   editor::GPUSetEnv per-step readback (Game/editor.cpp:226)       -> env.readField(...)
+//   Game.ReadTable().readDWDFile(file) / readKNMIFile(file) / initEnvironment()
+//       (Game/gameSystem.cpp:43-47)  -> table.readDWDFile(file, reader, ctx) / ... / table.initEnvironment(env)
 #pragma once
 
 #include <cstdint>
@@ -30,6 +32,7 @@ public:
         skt_grid_desc g{nx, ny_vertical, nz, voxel};
         check(skt_create(&g, cfg, &env_), nullptr);
         n_ = size_t(nx) * ny_vertical * nz;
+        grid_ = g;
     }
     ~EnvironmentGPU() { skt_destroy(env_); }
     EnvironmentGPU(const EnvironmentGPU&) = delete;
@@ -73,6 +76,7 @@ public:
     }
 
     skt_env* handle() { return env_; }
+    const skt_grid_desc& grid() const { return grid_; }
 
 private:
     void check(skt_status s, const skt_env* e = reinterpret_cast<const skt_env*>(1)) {
@@ -81,6 +85,49 @@ private:
     }
     skt_env* env_ = nullptr;
     size_t n_ = 0;
+    skt_grid_desc grid_{};
+};
+
+// readTable (Game/readTable.h:50-92), reading side. The reference opens the archive with
+// miniz_cpp::zip_file; here the caller's zip library answers member reads (skt_archive_read_fn).
+class ReadTable {
+public:
+    ReadTable() = default;
+    ~ReadTable() { skt_sounding_free(&data_); }
+    ReadTable(const ReadTable&) = delete;
+    ReadTable& operator=(const ReadTable&) = delete;
+
+    // readTable::readKNMIFile (Game/readTable.cpp:27-132)
+    void readKNMIFile(skt_archive_read_fn read, void* ctx) {
+        skt_sounding_free(&data_);
+        check(skt_sounding_read_knmi(read, ctx, &data_));
+    }
+
+    // readTable::readDWDFile (Game/readTable.cpp:134-354); file is the archive's path string
+    void readDWDFile(const char* file, skt_archive_read_fn read, void* ctx) {
+        skt_sounding_free(&data_);
+        check(skt_sounding_read_dwd(file, read, ctx, &data_));
+    }
+
+    // readTable::initEnvironment (Game/readTable.cpp:364-474): interpolate onto env's grid and
+    // call env.init with the result (flat ground).
+    void initEnvironment(EnvironmentGPU& env, bool noise = true, uint32_t seed = 100) {
+        const skt_grid_desc& g = env.grid();
+        const size_t n = size_t(g.nx) * g.ny * g.nz, ng = size_t(g.nx) * g.nz;
+        std::vector<float> theta(n), vel(3 * n), qv(n), gT(ng), gp(ng), p3d(n), pcol(g.ny);
+        check(skt_sounding_to_init(&data_, &g, theta.data(), vel.data(), qv.data(), gT.data(), gp.data(), p3d.data(),
+                                   pcol.data()));
+        std::vector<int32_t> gh(ng, 0);
+        env.init(theta.data(), vel.data(), qv.data(), gT.data(), gp.data(), p3d.data(), pcol.data(), gh.data(), noise, seed);
+    }
+
+    const skt_sounding& data() const { return data_; }
+
+private:
+    static void check(skt_status s) {
+        if (s != SKT_OK) throw Error(s, skt_last_error(nullptr));
+    }
+    skt_sounding data_{};
 };
 
 }  // namespace skewt

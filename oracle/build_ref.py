@@ -121,6 +121,58 @@ def build_harness(force: bool = False) -> str:
     return so
 
 
+# (X, Y vertical, Z, voxel): compile-time grids of the reference's sounding reader builds. The
+# first is the reference's own Game/config.h; 37.5 m makes the level heights non-integer.
+READTABLE_GRIDS = [(32, 32, 32, 64.0), (6, 40, 4, 100.0), (5, 24, 3, 37.5)]
+
+
+def readtable_path(X, Y, Z, voxel):
+    return os.path.join(OUT, f"libreadtable_{X}x{Y}x{Z}_{voxel:g}.so")
+
+
+def build_readtable(force: bool = False):
+    """The reference's sounding reader (Game/readTable.cpp with Engine/source/math/meteoformulas.cpp),
+    unmodified, as one shared library per compile-time grid, with the harness
+    ``oracle/ref_readtable.cpp`` appended. Host code only (g++), x86 or Arm."""
+    if not os.path.exists(os.path.join(REF, "Game", "readTable.cpp")):
+        return []
+    os.makedirs(OUT, exist_ok=True)
+    g = os.path.join(REF, "Game")
+    inc = ["-I", os.path.join(HERE, "readtable_stubs"), "-I", os.path.join(REF, "Engine", "include"),
+           "-I", os.path.join(REF, "Engine", "external"), "-I", g, "-I", os.path.join(CUDA_HOME, "include")]
+    # -fpermissive: zip_file.hpp passes a uint64_t callback where miniz wants mz_uint64, the
+    # same width under a different name on LP64 Linux
+    flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-w", "-fpermissive"]
+    meteo = os.path.join(OUT, "meteoformulas.o")
+    harness = os.path.join(HERE, "ref_readtable.cpp")
+    if force or not os.path.exists(meteo):
+        subprocess.run(["g++", *flags, *inc, "-c", os.path.join(REF, "Engine", "source", "math", "meteoformulas.cpp"),
+                        "-o", meteo + ".tmp"], check=True, capture_output=True, text=True)
+        os.replace(meteo + ".tmp", meteo)
+    outs = []
+    for X, Y, Z, vox in READTABLE_GRIDS:
+        so = readtable_path(X, Y, Z, vox)
+        outs.append(so)
+        if os.path.exists(so) and not force and os.path.getmtime(so) >= os.path.getmtime(harness):
+            continue
+        wrap = os.path.join(OUT, f"wrap_readtable_{X}x{Y}x{Z}_{vox:g}.cpp")
+        with open(wrap, "w") as f:
+            f.write(f'#include "{g}/config.h"\n')
+            for n, v in (("GRIDSIZESKYX", X), ("GRIDSIZESKYY", Y), ("GRIDSIZESKYZ", Z)):
+                f.write(f"#undef {n}\n#define {n} {v}\n")
+            f.write(f"#undef VOXELSIZE\n#define VOXELSIZE {vox}f\n")
+            # the reference was written against MSVC's headers: std::memset/strlen without
+            # <cstring>, std::sinf/cosf, which libstdc++ leaves in the global namespace
+            f.write("#include <cstring>\n#include <cmath>\nnamespace std { using ::sinf; using ::cosf; }\n")
+            f.write(f'#include "{g}/readTable.cpp"\n#include "{harness}"\n')
+        r = subprocess.run(["g++", *flags, "-shared", *inc, wrap, meteo, "-o", so + ".tmp"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference sounding reader build failed:\n{r.stderr[-4000:]}")
+        os.replace(so + ".tmp", so)
+    return outs
+
+
 if __name__ == "__main__":
     print(build_cubins(force=True))
     print(build_harness(force=True))
+    print(build_readtable(force=True))

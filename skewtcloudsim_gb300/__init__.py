@@ -2,11 +2,13 @@
 
 The compute path is libskewt_gb300.so (hand-written CUDA for sm_103a behind the C ABI in
 include/skewt.h). This package holds the host-side mirror of the reference's environmentGPU
-(``Environment``), the synthetic sounding generator and the build recipe.
+(``Environment``), the synthetic sounding generator, the radiosonde readers (``radiosonde``)
+and the build recipe.
 """
 from .environment import (Environment, SolverConfig, Parameter, Direction, Ground, Column, Status,
                           SktError, FIELDS, GROUND_FIELDS, COLUMNS, DIAG_BUOYANCY, RATE_NAMES)
 from . import sounding
+from . import radiosonde
 
-__all__ = ["Environment", "SolverConfig", "Parameter", "Direction", "Ground", "Column", "Status", "SktError",
+__all__ = ["radiosonde", "Environment", "SolverConfig", "Parameter", "Direction", "Ground", "Column", "Status", "SktError",
            "FIELDS", "GROUND_FIELDS", "COLUMNS", "DIAG_BUOYANCY", "RATE_NAMES", "sounding"]

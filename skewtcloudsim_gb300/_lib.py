@@ -24,6 +24,15 @@ class SolverCfg(ctypes.Structure):
                 ("use_graph", ctypes.c_int), ("mg_half", ctypes.c_int)]
 
 
+class Sounding(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("altitude", c_float_p), ("pressure", c_float_p), ("temperature", c_float_p),
+                ("dew_point", c_float_p), ("wind_speed", c_float_p), ("wind_dir", c_float_p)]
+
+
+# long long (*)(void* ctx, const char* name, char* buf, size_t cap)
+ARCHIVE_READ_FN = ctypes.CFUNCTYPE(ctypes.c_longlong, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t)
+
+
 class StepStats(ctypes.Structure):
     _fields_ = [("pcg_iters", ctypes.c_int), ("pcg_residual", ctypes.c_float), ("pcg_converged", ctypes.c_int),
                 ("nsub", ctypes.c_int * 10), ("outer_iters", ctypes.c_int), ("sim_time", ctypes.c_double),
@@ -68,6 +77,11 @@ SIGNATURES = {
                                            ctypes.c_float, c_float_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "skt_reset_parameter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "skt_read_ground_height": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_size_t]),
+    "skt_sounding_read_knmi": (ctypes.c_int, [ARCHIVE_READ_FN, ctypes.c_void_p, ctypes.POINTER(Sounding)]),
+    "skt_sounding_read_dwd": (ctypes.c_int, [ctypes.c_char_p, ARCHIVE_READ_FN, ctypes.c_void_p, ctypes.POINTER(Sounding)]),
+    "skt_sounding_free": (None, [ctypes.POINTER(Sounding)]),
+    "skt_sounding_to_init": (ctypes.c_int, [ctypes.POINTER(Sounding), ctypes.POINTER(GridDesc), c_float_p, c_float_p,
+                                            c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     "skt_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "skt_version": (ctypes.c_char_p, []),
 }

@@ -17,7 +17,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libskewt_gb300.so")
 ROOT = os.path.dirname(HERE)
 
-SOURCES = ["skt_api.cu", "skt_stencil.cu", "skt_project.cu", "skt_micro.cu", "skt_mg.cu", "skt_edit.cu"]
+SOURCES = ["skt_api.cu", "skt_stencil.cu", "skt_project.cu", "skt_micro.cu", "skt_mg.cu", "skt_edit.cu",
+           "skt_sounding.cu"]
+# host arithmetic that must round like the reference's (no fused multiply-add contraction)
+PER_SOURCE = {"skt_sounding.cu": ["-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC]
@@ -43,7 +46,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nv, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nv, *ARCH, *NVCC_FLAGS, *PER_SOURCE.get(src, []), *extra_flags, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
