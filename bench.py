@@ -51,6 +51,7 @@ STAGE_BYTES = {
     "diffuse": 8.0,       # per sweep: in read, out write
     "advect": 12.0,       # per pass: q, vel read; out write
     "micro": 64.0,        # 6 Q + th read/write, rho, p read (fused addHeat)
+    "precip": 36.0,       # qr, qs, qi read+write; th, qv, p read (one march for the three species)
     "buoyancy": 36.0,
     "eos": 16.0,
     "proj_setup": 48.0,
@@ -200,13 +201,14 @@ def run_reference(args, rank, world):
 
 def step_bytes(mode, pcg_iters, outer):
     """Algorithmic bytes per cell-step of the whole step (FP32, one advection substep): the stage
-    total of the hot-path scope (2558 B) plus the pressure solve. Plain Jacobi-PCG: 52 B per
+    total of the hot-path scope (2534 B; the three falling species share one march, 36 B instead
+    of 3 x 20) plus the pressure solve. Plain Jacobi-PCG: 52 B per
     iteration. Mixed: per inner iteration the operator + search (32 B), the update (24 B) and the
     V-cycle (93 B: four finest-level passes of 16-24.5 B with FP16 coefficients plus the coarser
     levels), per refinement step the float-float residual (32 B) and the correction (20 B)."""
     if mode == "plain":
-        return 2558.0 + 52.0 * pcg_iters
-    return 2558.0 + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
+        return 2534.0 + 52.0 * pcg_iters
+    return 2534.0 + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
 
 
 def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):

@@ -57,8 +57,9 @@ typedef enum {
     SKT_G_CLOUD_COVER = 7
 } skt_ground_field;
 
-/* Per-level default columns (ny values) taken at init. */
-typedef enum { SKT_C_ISEN_T = 0, SKT_C_ISEN_QV = 1, SKT_C_DEF_U = 2, SKT_C_DEF_W = 3 } skt_column;
+/* Per-level default columns (ny values) taken at init; SKT_C_PRESSURE is the pressure column
+ * skt_init received (the editor's pressure reset, m_defaultPressure). */
+typedef enum { SKT_C_ISEN_T = 0, SKT_C_ISEN_QV = 1, SKT_C_DEF_U = 2, SKT_C_DEF_W = 3, SKT_C_PRESSURE = 4 } skt_column;
 
 typedef struct {
     int nx, ny, nz; /* ny is vertical */
@@ -289,6 +290,37 @@ void skt_sounding_free(skt_sounding* s);
  * SKT_INVALID_ARG when the sounding ends below the grid top. */
 skt_status skt_sounding_to_init(const skt_sounding* s, const skt_grid_desc* grid, float* theta, float* vel_aos3,
                                 float* qv, float* ground_T, float* ground_p, float* p3d, float* p_column);
+
+/* ---- Headless view and volume export (the editor's voxel view, without a renderer) ---- */
+
+#define SKT_VOXEL_HIDDEN 0         /* not drawn */
+#define SKT_VOXEL_SKY 1            /* a sky voxel in the view's colour */
+#define SKT_VOXEL_GROUND 2         /* ground below the surface (brown) */
+#define SKT_VOXEL_GROUND_SURFACE 3 /* the surface voxel of a column, in the ground view's colour */
+
+/* Replaces the per-frame voxel drawing of editor::viewSky and editor::viewGround
+ * (Game/editor.cpp:1041-1171) with the colour schemes of editor::setColors (:53-112), evaluated
+ * per cell on the device as bee::colorScheme::getColor does (Engine/source/rendering/colors.cpp:28-67).
+ * sky_param selects the sky view like the editor's buttons: SKT_POTTEMP (the temperature
+ * theta * (p / ground p)^(Rsd/Cpd)), SKT_QV..SKT_QI, SKT_WIND (the cell-centred speed of
+ * environment::getUV), SKT_PRESSURE, SKT_DEBUG1 (the "realistic" view of all condensate, cells
+ * below 1e-4 kg/kg not drawn), SKT_DEBUG2 and SKT_DEBUG3 (the debug fields). ground_param selects
+ * the ground view (0 temperature, 1 Qrs, 2 Qgr, 3 Qgs, 4 Qgi; -1 none). lo/hi (x, y, z, y vertical)
+ * bound the sky view like the editor's slice (NULL: the whole grid). Writes n = nx*ny*nz RGB
+ * triples (floats, 0..1) and voxel kinds (SKT_VOXEL_*) to host memory. Synchronous. */
+skt_status skt_view_volume(skt_env* env, int sky_param, int ground_param, const int lo[3], const int hi[3], float* rgb,
+                           uint8_t* kind, size_t n);
+
+/* Sparse export of one field (same selectors as skt_read_field) in bricks of 8x8x8 cells: a
+ * brick is written when one of its cells differs from `background` by more than `threshold`
+ * (NaN always; threshold < 0 writes every brick). Bricks go out in brick order (x fastest), each
+ * as 512 values in x-fastest order (cells past the grid edge hold the background), as float or,
+ * with half != 0, IEEE half (round to nearest even), with their brick coordinates (3 uint32 each).
+ * *count receives the number of bricks; nothing is copied when coords or values is NULL or
+ * capacity (in bricks) is below the count, so a first call with capacity 0 sizes the buffers.
+ * Synchronous. */
+skt_status skt_export_bricks(skt_env* env, int param, int dir, float background, float threshold, int half,
+                             uint32_t* coords, void* values, size_t capacity, size_t* count);
 
 /* Text of the last error on env (or, when env is NULL, of the last skt_create,
  * skt_diffuse_noalloc or skt_sounding_* failure on this thread). */

@@ -82,6 +82,12 @@ SIGNATURES = {
     "skt_sounding_free": (None, [ctypes.POINTER(Sounding)]),
     "skt_sounding_to_init": (ctypes.c_int, [ctypes.POINTER(Sounding), ctypes.POINTER(GridDesc), c_float_p, c_float_p,
                                             c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "skt_view_volume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_int), c_float_p, ctypes.POINTER(ctypes.c_uint8),
+                                       ctypes.c_size_t]),
+    "skt_export_bricks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_int, ctypes.POINTER(ctypes.c_uint32), ctypes.c_void_p, ctypes.c_size_t,
+                                         ctypes.POINTER(ctypes.c_size_t)]),
     "skt_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "skt_version": (ctypes.c_char_p, []),
 }

@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, "libskewt_gb300.so")
 ROOT = os.path.dirname(HERE)
 
 SOURCES = ["skt_api.cu", "skt_stencil.cu", "skt_project.cu", "skt_micro.cu", "skt_mg.cu", "skt_edit.cu",
-           "skt_sounding.cu"]
+           "skt_sounding.cu", "skt_export.cu"]
 # host arithmetic that must round like the reference's (no fused multiply-add contraction)
 PER_SOURCE = {"skt_sounding.cu": ["-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -89,6 +89,7 @@ float* column_ptr(Env& e, int which) {
         case SKT_C_ISEN_QV: return e.isenQv;
         case SKT_C_DEF_U: return e.defU;
         case SKT_C_DEF_W: return e.defW;
+        case SKT_C_PRESSURE: return e.pcol;
         default: return nullptr;
     }
 }
@@ -123,14 +124,14 @@ skt_status run_step(Env& e, float dt, float speed) {
     e.last_nsub[5] = launch_advect(e, e.qw, e.zeroY, DIRICHLET, DIRICHLET, dtS, 5, hs);
     launch_diffuse(e, e.qc, 5, dtS);
     e.last_nsub[6] = launch_advect(e, e.qc, e.zeroY, DIRICHLET, DIRICHLET, dtS, 6, hs);
+    // rain, snow and ice: diffuse, fall, advect each (the reference's order per species; the
+    // species do not read one another here, so the three falls run as one column march)
     launch_diffuse(e, e.qr, 5, dtS);
-    launch_precip(e, e.qr, 0, dtS);
-    e.last_nsub[7] = launch_advect(e, e.qr, e.zeroY, DIRICHLET, DIRICHLET, dtS, 7, hs);
     launch_diffuse(e, e.qs, 5, dtS);
-    launch_precip(e, e.qs, 1, dtS);
-    e.last_nsub[8] = launch_advect(e, e.qs, e.zeroY, DIRICHLET, DIRICHLET, dtS, 8, hs);
     launch_diffuse(e, e.qi, 5, dtS);
-    launch_precip(e, e.qi, 2, dtS);
+    launch_precip3(e, dtS);
+    e.last_nsub[7] = launch_advect(e, e.qr, e.zeroY, DIRICHLET, DIRICHLET, dtS, 7, hs);
+    e.last_nsub[8] = launch_advect(e, e.qs, e.zeroY, DIRICHLET, DIRICHLET, dtS, 8, hs);
     e.last_nsub[9] = launch_advect(e, e.qi, e.zeroY, DIRICHLET, DIRICHLET, dtS, 9, hs);
     // microphysics + latent heat
     launch_micro(e, dt, speed);
@@ -145,6 +146,8 @@ skt_status run_step(Env& e, float dt, float speed) {
 namespace skt {
 void set_global_error(const char* msg) { g_create_err = msg ? msg : ""; }
 skt_status report(Env* e, skt_status st, const char* msg) { return fail(e, st, msg); }
+float* field_ptr(Env& e, int param, int dir) { return sky_ptr(e, param, dir); }
+float* ground_field_ptr(Env& e, int which) { return ground_ptr(e, which); }
 skt_status check_cuda(Env& e, const char* where) { return cuda_check(e, where); }
 }  // namespace skt
 
@@ -337,6 +340,8 @@ void skt_destroy(skt_env* env) {
     if (e.rates_dev) cudaFree(e.rates_dev);
     if (e.dbg_buoy) cudaFree(e.dbg_buoy);
     if (e.dbg_zero) cudaFree(e.dbg_zero);
+    if (e.brick_flags) cudaFree(e.brick_flags);
+    if (e.brick_out) cudaFree(e.brick_out);
     if (e.host_sc) cudaFreeHost(e.host_sc);
     if (e.stream) cudaStreamDestroy(e.stream);
     delete env;

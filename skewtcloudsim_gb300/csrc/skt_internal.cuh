@@ -164,6 +164,11 @@ struct Env {
     int rates_on = 0;
     int rate_lo[3] = {0, 0, 0}, rate_hi[3] = {0, 0, 0};
     double* rates_dev = nullptr;  // the 33 region-summed process amounts of the last step
+    // volume export scratch (allocated by the first export, never during a step)
+    int* brick_flags = nullptr;   // per 8^3 brick: active, then its output slot
+    int* brick_count = nullptr;
+    void* brick_out = nullptr;    // packed brick values and coordinates
+    size_t brick_out_bytes = 0;
     int diag_flags = 0;
     float* dbg_buoy = nullptr;    // buoyancy velocity change per cell (the second debug field)
     float* dbg_zero = nullptr;    // the first debug field, which the step never writes
@@ -199,6 +204,7 @@ struct ProfScope {
 void launch_diffuse(Env& e, float* f, int type, float dtS);
 int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int field_slot, bool host_sync);
 void launch_precip(Env& e, float* q, int type, float dtS);
+void launch_precip3(Env& e, float dtS);  // rain, snow and ice in one column march
 void launch_buoyancy(Env& e, float dtS);
 void launch_init_density(Env& e);
 void launch_new_pressure(Env& e);
@@ -216,6 +222,9 @@ void mg_solve(Env& e);
 // create error) and return st; turn a pending CUDA error into a status
 skt_status report(Env* e, skt_status st, const char* msg);
 skt_status check_cuda(Env& e, const char* where);
+// the device array behind a field selector (skt_read_field's mapping), nullptr if none
+float* field_ptr(Env& e, int param, int dir);
+float* ground_field_ptr(Env& e, int which);
 
 }  // namespace skt
 

@@ -67,10 +67,20 @@ constexpr int DVY = 4;
 __device__ __forceinline__ float4 ld4f(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
 __device__ __forceinline__ float side_val(int bc, float own, float d) { return bc == NEUMANN ? own : (bc == DIRICHLET ? 0.0f : d); }
 
+// theta's ground-face values of the first sky row (theta_ground), once per diffusion call: they
+// depend on p, Tg and Pg only, which the sweeps do not change
+__global__ void __launch_bounds__(256) k_theta_face(Grid g, const float* __restrict__ p, const float* __restrict__ Tg,
+                                                    const float* __restrict__ Pg, float* __restrict__ face) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.X * g.Z) return;
+    face[col] = theta_ground(p, Tg, Pg, cidx(g, col % g.X, 1, col / g.X), col);
+}
+
+// face: theta's ground-face values per column (k_theta_face), read at the first sky row
 template <bool THETA>
 __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out, int sides,
-                                                       int ground, const float* __restrict__ def, float k, const float* __restrict__ p,
-                                                       const float* __restrict__ Tg, const float* __restrict__ Pg) {
+                                                       int ground, const float* __restrict__ def, float k,
+                                                       const float* __restrict__ face) {
     const int lane = threadIdx.x;
     const int x0 = (blockIdx.x * 32 + lane) * 4;
     const int y = blockIdx.y * DVY + threadIdx.y + 1;  // sky rows start at y = 1
@@ -106,13 +116,7 @@ __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const f
         if (act) {
             if (lane == 0) ql = x0 > 0 ? in[c - 1] : side_val(sides, qc.x, dy);
             if (lane == 31 || x0 + 4 >= X) qr = (x0 + 4 < X) ? in[c + 4] : side_val(sides, qc.w, dy);
-            if (THETA && y == 1) {  // theta's ground face (diffuseRedBlack :97)
-                const int gi = x0 + z * X;
-                qd.x = theta_ground(p, Tg, Pg, c, gi);
-                qd.y = theta_ground(p, Tg, Pg, c + 1, gi + 1);
-                qd.z = theta_ground(p, Tg, Pg, c + 2, gi + 2);
-                qd.w = theta_ground(p, Tg, Pg, c + 3, gi + 3);
-            }
+            if (THETA && y == 1) qd = ld4f(face, x0 + z * X);  // theta's ground face (diffuseRedBlack :97)
             float4 o;
             o.x = (qc.x + k * (ql + qc.y + qu.x + qd.x + qf.x + qb.x)) * rinv;
             o.y = (qc.y + k * (qc.x + qc.z + qu.y + qd.y + qf.y + qb.y)) * rinv;
@@ -228,8 +232,11 @@ __device__ __forceinline__ float ppm_cdt(const Grid& g, float dtFull, int nsub, 
 }
 
 // Vectorised X pass (flat terrain, X % 4 == 0): a thread owns four cells of one row and marches
-// z. Its four upper-face fluxes use the x window q(x0-2) .. q(x0+5); the lower face of its first
-// cell is the upper face of the lane before it (a shuffle), computed directly by lane 0.
+// z. Its four upper-face fluxes use the x window q(x0-1) .. q(x0+5); the lower face of its first
+// cell is the upper face of the lane before it (a shuffle). For lane 0 that face lies in the
+// previous warp's cells: its flux (and q(x0-1)) is computed for 32 planes at once, one plane per
+// lane, and handed to lane 0 plane by plane, so the warp does not spend a whole flux evaluation
+// per plane on one lane.
 __global__ void __launch_bounds__(32 * DVY) k_ppm4x(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
                                                     const float* __restrict__ vel, const float* __restrict__ def, int sides,
                                                     const float* __restrict__ defU, float dtFull, int nsub_host, int half,
@@ -241,58 +248,73 @@ __global__ void __launch_bounds__(32 * DVY) k_ppm4x(Grid g, int zlen, const floa
     }
     const float cdt = ppm_cdt(g, dtFull, nsub, half);
     const int lane = threadIdx.x;
-    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int xw = blockIdx.x * 128;  // the warp's first cell
+    const int x0 = xw + lane * 4;
     const int y = blockIdx.y * DVY + threadIdx.y + 1;
     const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool wact = xw < g.X && y < g.Y;  // same for every lane of the warp
     const bool act = x0 < g.X && y < g.Y;
     const int X = g.X, XY = g.XY;
-    const int row = x0 + y * X;
-    const float dy = act ? (def ? def[y] : 0.0f) : 0.0f;
-    const float du = act ? defU[y] : 0.0f;
+    const int row = x0 + y * X, roww = xw + y * X;
+    const float dy = wact ? (def ? def[y] : 0.0f) : 0.0f;
+    const float du = wact ? defU[y] : 0.0f;
     const float so = bc_val(sides, 1.0f, 1.0f);
     const bool xedge = x0 < 4 || x0 + 8 > X;  // the companion window reaches outside the domain
+    const bool xedge0 = xw < 4 || xw + 8 > X;
     auto ow = [&](int j) { return (x0 - 2 + j >= 0 && x0 - 2 + j < X) ? 1.0f : so; };
-    for (int z = zs; z < ze; ++z) {
-        const int c = row + z * XY;
-        float4 qc = make_float4(0, 0, 0, 0), uc = qc;
-        if (act) { qc = ld4f(in, c); uc = ld4f(vel, c); }
-        float qm2 = __shfl_up_sync(0xffffffffu, qc.z, 1), qm1 = __shfl_up_sync(0xffffffffu, qc.w, 1);
-        float qp4 = __shfl_down_sync(0xffffffffu, qc.x, 1), qp5 = __shfl_down_sync(0xffffffffu, qc.y, 1);
-        float um1 = __shfl_up_sync(0xffffffffu, uc.w, 1);
-        if (act && lane == 0) {
-            if (x0 >= 4) { qm2 = in[c - 2]; qm1 = in[c - 1]; um1 = vel[c - 1]; }
-            else { qm2 = qm1 = bc_val(sides, qc.x, dy); um1 = bc_val(sides, uc.x, du); }
+    auto ow0 = [&](int j) { return (xw - 2 + j >= 0 && xw - 2 + j < X) ? 1.0f : so; };
+    for (int zb = zs; zb < ze; zb += 32) {
+        // the warp's lower boundary face for planes zb .. zb+31: plane zb + lane on this lane
+        float Bq = 0.0f, BF = 0.0f, BFo = 0.0f;
+        if (wact && zb + lane < ze) {
+            const int cw = roww + (zb + lane) * XY;
+            const float a2 = in[cw], a3 = in[cw + 1];
+            float a0, um;
+            if (xw >= 4) { a0 = in[cw - 2]; Bq = in[cw - 1]; um = vel[cw - 1]; }
+            else { a0 = Bq = bc_val(sides, a2, dy); um = bc_val(sides, vel[cw], du); }
+            BF = face_flux(um, a0, Bq, a2, a3, cdt);
+            BFo = xedge0 ? face_flux(um, ow0(0), ow0(1), ow0(2), ow0(3), cdt) : um;
         }
-        if (act && (lane == 31 || x0 + 4 >= X)) {
-            if (x0 + 4 < X) { qp4 = in[c + 4]; qp5 = in[c + 5]; }
-            else { qp4 = qp5 = bc_val(sides, qc.w, dy); }
-        }
-        const float w[8] = {qm2, qm1, qc.x, qc.y, qc.z, qc.w, qp4, qp5};
-        const float u[4] = {uc.x, uc.y, uc.z, uc.w};
-        float F[4], Fo[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            F[k] = face_flux(u[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], cdt);
-            Fo[k] = u[k];
-        }
-        if (xedge) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) Fo[k] = face_flux(u[k], ow(k + 1), ow(k + 2), ow(k + 3), ow(k + 4), cdt);
-        }
-        float Fm = __shfl_up_sync(0xffffffffu, F[3], 1);
-        float Fmo = __shfl_up_sync(0xffffffffu, Fo[3], 1);
-        if (lane == 0) {
-            Fm = face_flux(um1, w[0], w[1], w[2], w[3], cdt);
-            Fmo = xedge ? face_flux(um1, ow(0), ow(1), ow(2), ow(3), cdt) : um1;
-        }
-        if (act) {
-            float4 o4;
+        const int zend = min(zb + 32, ze);
+        for (int z = zb; z < zend; ++z) {
+            const int c = row + z * XY;
+            float4 qc = make_float4(0, 0, 0, 0), uc = qc;
+            if (act) { qc = ld4f(in, c); uc = ld4f(vel, c); }
+            const int src = z - zb;
+            const float bq = __shfl_sync(0xffffffffu, Bq, src);
+            const float bf = __shfl_sync(0xffffffffu, BF, src);
+            const float bfo = __shfl_sync(0xffffffffu, BFo, src);
+            float qm1 = __shfl_up_sync(0xffffffffu, qc.w, 1);
+            float qp4 = __shfl_down_sync(0xffffffffu, qc.x, 1), qp5 = __shfl_down_sync(0xffffffffu, qc.y, 1);
+            if (lane == 0) qm1 = bq;
+            if (act && (lane == 31 || x0 + 4 >= X)) {
+                if (x0 + 4 < X) { qp4 = in[c + 4]; qp5 = in[c + 5]; }
+                else { qp4 = qp5 = bc_val(sides, qc.w, dy); }
+            }
+            const float w[7] = {qm1, qc.x, qc.y, qc.z, qc.w, qp4, qp5};
+            const float u[4] = {uc.x, uc.y, uc.z, uc.w};
+            float F[4], Fo[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float fm = k == 0 ? Fm : F[k - 1], fmo = k == 0 ? Fmo : Fo[k - 1];
-                setc(o4, k, ppm_update(w[k + 2], F[k], fm, Fo[k], fmo, cdt));
+                F[k] = face_flux(u[k], w[k], w[k + 1], w[k + 2], w[k + 3], cdt);
+                Fo[k] = u[k];
             }
-            *reinterpret_cast<float4*>(out + c) = o4;
+            if (xedge) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) Fo[k] = face_flux(u[k], ow(k + 1), ow(k + 2), ow(k + 3), ow(k + 4), cdt);
+            }
+            float Fm = __shfl_up_sync(0xffffffffu, F[3], 1);
+            float Fmo = __shfl_up_sync(0xffffffffu, Fo[3], 1);
+            if (lane == 0) { Fm = bf; Fmo = bfo; }
+            if (act) {
+                float4 o4;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float fm = k == 0 ? Fm : F[k - 1], fmo = k == 0 ? Fmo : Fo[k - 1];
+                    setc(o4, k, ppm_update(w[k + 1], F[k], fm, Fo[k], fmo, cdt));
+                }
+                *reinterpret_cast<float4*>(out + c) = o4;
+            }
         }
     }
 }
@@ -547,6 +569,81 @@ __global__ void __launch_bounds__(128) k_precip(Grid g, float* __restrict__ q, c
     }
 }
 
+// The three falling species in one column march: precipGPU for rain, snow and ice
+// (Game/kernelSky.cu:576-657, one launch per species in the reference). A species touches only its
+// own mixing ratio and every species of a cell uses the same temperature, virtual temperature and
+// density, so the three marches are one here, with each species' arithmetic unchanged. mask selects
+// the species of this march (a species with more Courant substeps gets further marches). The
+// loads of the row two above are issued one iteration ahead.
+__device__ __forceinline__ float precip_dens(float thv, float qvv, float pv, float pgc) {
+    const float T = thv * powf(pv / pgc, KC::KAPPA);
+    const float Tv = T * (0.608f * qvv + 1);
+    return pv * 100 / (KC::Rsd * Tv);
+}
+__device__ __forceinline__ float precip_speed(float Q, float dens, int type, const Gammas& G) {
+    float UR, US, UI;
+    fallingVelocity(Q, Q, Q, dens, type, G.Qr, G.Qs, G.Qi, UR, US, UI);
+    return type == 0 ? UR : (type == 1 ? US : UI);
+}
+__global__ void __launch_bounds__(128) k_precip3(Grid g, float* __restrict__ qr, float* __restrict__ qs, float* __restrict__ qi,
+                                                 const float* __restrict__ th, const float* __restrict__ qv,
+                                                 const float* __restrict__ p, const float* __restrict__ Pg, int mask, float dtr,
+                                                 float dts, float dti, Gammas G) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.X * g.Z) return;
+    const int x = col % g.X, z = col / g.X;
+    int y = max(g.gh[col] + 1, 0);
+    if (y >= g.Y) return;
+    float* const qs3[3] = {qr, qs, qi};
+    const float dt3[3] = {dtr, dts, dti};
+    const float vox = g.vox, pgc = Pg[col];
+    const int X = g.X;
+    int c = cidx(g, x, y, z);
+    float QC[3] = {0.0f, 0.0f, 0.0f}, fv[3] = {0.0f, 0.0f, 0.0f};
+    {
+        const float d = precip_dens(th[c], qv[c], p[c], pgc);
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (mask & (1 << t)) { QC[t] = qs3[t][c]; fv[t] = precip_speed(QC[t], d, t, G); }
+    }
+    // the row above, loaded ahead
+    float thN = 0.0f, qvN = 0.0f, pN = 0.0f, QN[3] = {0.0f, 0.0f, 0.0f};
+    if (y + 1 < g.Y) {
+        thN = th[c + X]; qvN = qv[c + X]; pN = p[c + X];
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (mask & (1 << t)) QN[t] = qs3[t][c + X];
+    }
+    for (; y < g.Y; ++y) {
+        const bool up = y < g.Y - 1;
+        float QU[3] = {0.0f, 0.0f, 0.0f}, fvu[3] = {0.0f, 0.0f, 0.0f};
+        if (up) {
+            const float d = precip_dens(thN, qvN, pN, pgc);
+#pragma unroll
+            for (int t = 0; t < 3; ++t)
+                if (mask & (1 << t)) { QU[t] = QN[t]; fvu[t] = precip_speed(QU[t], d, t, G); }
+        }
+        if (y + 2 < g.Y) {
+            const int c2 = c + 2 * X;
+            thN = th[c2]; qvN = qv[c2]; pN = p[c2];
+#pragma unroll
+            for (int t = 0; t < 3; ++t)
+                if (mask & (1 << t)) QN[t] = qs3[t][c2];
+        }
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            if (!(mask & (1 << t))) continue;
+            float val = QC[t];
+            val -= dt3[t] * fminf((fv[t] / vox) * QC[t], QC[t]);
+            if (up) val += dt3[t] * fminf((fvu[t] / vox) * QU[t], QU[t]);
+            qs3[t][c] = val;
+            QC[t] = QU[t];
+            fv[t] = fvu[t];
+        }
+        c += X;
+    }
+}
+
 // buoyancyGPU Game/kernelSky.cu:1061-1247 (bounds DIRICHLET everywhere)
 __global__ void __launch_bounds__(256) k_buoyancy(Grid g, float* __restrict__ v, const float* __restrict__ th, const float* __restrict__ qv,
                                                   const float* __restrict__ qr, const float* __restrict__ qs, const float* __restrict__ qi,
@@ -660,12 +757,17 @@ void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float*
     vz = (g.Z + vlen - 1) / vlen;
     float* buf[2] = {e.tA, e.tB};
     const float* src = f;
+    float* face = e.g2a;  // ground scratch: free until the ground stage refills it
+    if (type == 0) {
+        k_theta_face<<<(g.X * g.Z + 255) / 256, 256, 0, e.stream>>>(g, e.p, e.Tg, e.Pg, face);
+        e.launches += 1;
+    }
     for (int q = 0; q < sweeps; ++q) {
         float* dst = (q == sweeps - 1 && q > 0) ? f : buf[q % 2];
         if (type == 0)
-            k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, e.p, e.Tg, e.Pg);
+            k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, face);
         else
-            k_diffuse4<false><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, e.p, e.Tg, e.Pg);
+            k_diffuse4<false><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, nullptr);
         e.launches += 1;
         src = dst;
     }
@@ -704,21 +806,11 @@ void launch_diffuse(Env& e, float* f, int type, float dtS) {
     cudaMemcpyAsync(e.tB, f, sizeof(float) * size_t(g.N), cudaMemcpyDeviceToDevice, e.stream);
     float* a = e.tA;
     float* o = e.tB;
+    // general heightfield or X % 4 != 0 (or no sweeps): the scalar sweep
     const bool vec = e.flat && (g.X % 4) == 0;
-    const int gx = (g.X / 4 + 31) / 32, gy = (g.Y - 1 + DVY - 1) / DVY;
-    int zc = std::max(1, std::min(g.Z, (e.num_sms * 16 + gx * gy - 1) / (gx * gy)));
-    const int zlen = (g.Z + zc - 1) / zc;
-    zc = (g.Z + zlen - 1) / zlen;
     for (int s = 0; s < sweeps; ++s) {
         const float* in = (s % 2 == 0) ? a : o;
         float* out = (s % 2 == 0) ? o : a;
-        if (vec) {
-            if (type == 0)
-                k_diffuse4<true><<<dim3(gx, gy, zc), dim3(32, DVY), 0, e.stream>>>(g, zlen, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
-            else
-                k_diffuse4<false><<<dim3(gx, gy, zc), dim3(32, DVY), 0, e.stream>>>(g, zlen, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
-            continue;
-        }
         if (type == 0)
             k_diffuse<true><<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, in, out, sides, ground, def, k, e.p, e.Tg, e.Pg);
         else
@@ -844,6 +936,29 @@ void launch_precip(Env& e, float* q, int type, float dtS) {
     e.launches += sub;
     for (int i = 0; i < sub; ++i)
         k_precip<<<(cols + 127) / 128, 128, 0, e.stream>>>(g, q, e.th, e.qv, e.p, e.Pg, type, dts, e.gam);
+}
+
+// rain, snow and ice with their own Courant substeps (maximum fall speeds 5, 1, 8 m/s as in
+// launch_precip); march s updates the species that need more than s substeps
+void launch_precip3(Env& e, float dtS) {
+    const Grid& g = e.g;
+    const float maxVel[3] = {5.0f, 1.0f, 8.0f};
+    int sub[3], passes = 0;
+    float dts[3];
+    for (int t = 0; t < 3; ++t) {
+        const float C = maxVel[t] * dtS / g.vox;
+        sub[t] = int(fminf(ceilf(fabsf(C)), float(e.cfg.max_substeps)));
+        dts[t] = dtS / float(sub[t]);
+        passes = std::max(passes, sub[t]);
+    }
+    const int cols = g.X * g.Z;
+    ProfScope ps(e, "precip");
+    for (int s = 0; s < passes; ++s) {
+        const int mask = (sub[0] > s ? 1 : 0) | (sub[1] > s ? 2 : 0) | (sub[2] > s ? 4 : 0);
+        e.launches += 1;
+        k_precip3<<<(cols + 127) / 128, 128, 0, e.stream>>>(g, e.qr, e.qs, e.qi, e.th, e.qv, e.p, e.Pg, mask, dts[0], dts[1],
+                                                            dts[2], e.gam);
+    }
 }
 
 void launch_buoyancy(Env& e, float dtS) {

@@ -73,6 +73,7 @@ class Column(IntEnum):
     ISEN_QV = 1
     DEF_U = 2
     DEF_W = 3
+    PRESSURE = 4
 
 
 class SktError(RuntimeError):
@@ -98,7 +99,8 @@ RATE_NAMES = ("PVCON", "PVDEP", "PIMLT", "PIDW", "PIHOM", "PIACR", "PRACI", "PRA
               "PGACR", "PGDRY", "PGACS", "PGSUB", "PGMLT", "PGWET", "PGACR1", "PVVAP", "PVSUB")
 GROUND_FIELDS = {"Qrs": Ground.QRS, "Qgr": Ground.QGR, "Qgs": Ground.QGS, "Qgi": Ground.QGI, "Pg": Ground.P,
                  "tg": Ground.TIME_WET, "Tg": Ground.T, "cover": Ground.CLOUD_COVER}
-COLUMNS = {"isenT": Column.ISEN_T, "isenQv": Column.ISEN_QV, "defU": Column.DEF_U, "defW": Column.DEF_W}
+COLUMNS = {"isenT": Column.ISEN_T, "isenQv": Column.ISEN_QV, "defU": Column.DEF_U, "defW": Column.DEF_W,
+           "pcol": Column.PRESSURE}
 
 
 @dataclass
@@ -141,6 +143,7 @@ class Environment:
         if st != 0:
             raise SktError(st, self._L.skt_last_error(None).decode())
         self._h = h
+        self._clock = dict(day=130, longitude=52.37, sun=1.0, pause=0)
 
     # -- lifetime --------------------------------------------------------------------------
     def close(self):
@@ -239,6 +242,21 @@ class Environment:
 
     def set_clock(self, sim_time=43200.0, day=130, longitude=52.37, sun=1.0, pause=0):
         self._check(self._L.skt_set_clock(self._h, sim_time, day, longitude, sun, pause))
+        self._clock = dict(day=day, longitude=longitude, sun=sun, pause=pause)
+
+    # -- headless view, volume export, checkpoints (skewtcloudsim_gb300.volume) ----------------
+    def view(self, sky: int = Parameter.POTTEMP, ground: int = -1, lo=None, hi=None):
+        """The editor's voxel view: (rgb (n, 3) float32, kind (n,) uint8); see volume.view_volume."""
+        from . import volume
+        return volume.view_volume(self, sky, ground, lo, hi)
+
+    def export_bricks(self, name: str, threshold: float = 0.0, background: float = 0.0, half: bool = False):
+        from . import volume
+        return volume.export_bricks(self, name, threshold, background, half)
+
+    def save_checkpoint(self, path):
+        from . import volume
+        volume.save_checkpoint(self, path)
 
     def stats(self) -> dict:
         s = _lib.StepStats()

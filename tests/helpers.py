@@ -35,7 +35,8 @@ def push_oracle_to_env(st: oracle.OracleState, env: Environment):
     for k in GROUND:
         env.write(k, st.a[k].astype(np.float32))
     for k in COLUMNS:
-        env.write(k, st.a[k].astype(np.float32))
+        if k in st.a:  # the oracle holds no copy of the init pressure column
+            env.write(k, st.a[k].astype(np.float32))
     env.set_clock(st.sim_time, st.day, st.longitude, st.sun, st.pause)
 
 
