@@ -11,6 +11,7 @@
 
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cstring>
 
 namespace skt {
@@ -67,8 +68,8 @@ const Ramp kRamps[R_COUNT] = {
 // getColor: lower_bound on the keys; the end and the first key return a key colour; otherwise
 // Lerp (Engine/include/math/math.hpp:11-15) of the two neighbouring colours by the clamped
 // fraction, a * (1 - t) + b * t, every operation rounded on its own (no contraction).
-__device__ __forceinline__ void ramp_color(int which, float v, float* out) {
-    const Ramp& r = c_ramps[which];
+__device__ __forceinline__ void ramp_color(const Ramp* ramps, int which, float v, float* out) {
+    const Ramp& r = ramps[which];
     int it = 0;
     while (it < r.n && r.key[it] < v) it++;
     int pick = -1;
@@ -97,11 +98,20 @@ struct ViewArgs {
 };
 
 // editor::viewSky and viewGround for every cell. kind: 0 not drawn, 1 sky voxel, 2 ground below
-// the surface (brown), 3 the ground surface voxel (the ground view's colour).
-__global__ void __launch_bounds__(256) k_view(Grid g, ViewArgs a, float* __restrict__ rgb, uint8_t* __restrict__ kind) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.N; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)i;
-        const int x = c % g.X, y = (c / g.X) % g.Y, z = c / g.XY;
+// the surface (brown), 3 the ground surface voxel (the ground view's colour). A block covers 128
+// cells of one row and walks z; the schemes sit in shared memory (threads of a warp search them
+// at different keys, which constant memory would serve one address at a time).
+__global__ void __launch_bounds__(128) k_view(Grid g, ViewArgs a, float* __restrict__ rgb, uint8_t* __restrict__ kind) {
+    __shared__ Ramp ramps[R_COUNT];
+    for (int i = threadIdx.x; i < (int)(sizeof(ramps) / sizeof(int)); i += blockDim.x)
+        reinterpret_cast<int*>(ramps)[i] = reinterpret_cast<const int*>(c_ramps)[i];
+    __syncthreads();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    const int zlen = (g.Z + gridDim.z - 1) / gridDim.z, zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    if (x >= g.X) return;
+    for (int z = zs; z < ze; ++z) {
+        const int c = x + y * g.X + z * g.XY;
+        const long long i = c;
         const int cg = x + z * g.X;
         const int gh = g.gh[cg];
         float col[3] = {0.0f, 0.0f, 0.0f};
@@ -109,7 +119,7 @@ __global__ void __launch_bounds__(256) k_view(Grid g, ViewArgs a, float* __restr
         const bool in_box = x >= a.lo[0] && x < a.hi[0] && y >= a.lo[1] && y < a.hi[1] && z >= a.lo[2] && z < a.hi[2];
         if (y == gh) {
             if (a.gfield) {  // viewGround draws the surface voxel of every column
-                ramp_color(a.ground_param == 0 ? R_TEMP : R_MIX, a.gfield[cg], col);
+                ramp_color(ramps, a.ground_param == 0 ? R_TEMP : R_MIX, a.gfield[cg], col);
                 k = 3;
             }
         } else if (in_box && y < gh) {
@@ -123,15 +133,15 @@ __global__ void __launch_bounds__(256) k_view(Grid g, ViewArgs a, float* __restr
                     const float kappa = 287.0528f / 1003.5f;
                     const float f = powf(__fdiv_rn(a.p[c], a.Pg[cg]), kappa);
                     const float t = __fadd_rn(__fsub_rn(__fmul_rn(__fadd_rn(tz, 273.15f), f), 273.15f), 273.15f);
-                    ramp_color(R_TEMP, t, col);
+                    ramp_color(ramps, R_TEMP, t, col);
                     break;
                 }
-                case SKT_QV: ramp_color(R_MIX, a.qv[c], col); break;
-                case SKT_QW: ramp_color(R_MIX, a.qw[c], col); break;
-                case SKT_QC: ramp_color(R_MIX, a.qc[c], col); break;
-                case SKT_QR: ramp_color(R_MIX, a.qr[c], col); break;
-                case SKT_QS: ramp_color(R_MIX, a.qs[c], col); break;
-                case SKT_QI: ramp_color(R_MIX, a.qi[c], col); break;
+                case SKT_QV: ramp_color(ramps, R_MIX, a.qv[c], col); break;
+                case SKT_QW: ramp_color(ramps, R_MIX, a.qw[c], col); break;
+                case SKT_QC: ramp_color(ramps, R_MIX, a.qc[c], col); break;
+                case SKT_QR: ramp_color(ramps, R_MIX, a.qr[c], col); break;
+                case SKT_QS: ramp_color(ramps, R_MIX, a.qs[c], col); break;
+                case SKT_QI: ramp_color(ramps, R_MIX, a.qi[c], col); break;
                 case SKT_WIND: {  // |getUV| (Game/environment.cpp:2083-2095): the z term averages w
                                   // with the v of the cell behind, as the reference does
                     const float uc = a.u[c], vc = a.v[c], wc = a.w[c];
@@ -142,13 +152,13 @@ __global__ void __launch_bounds__(256) k_view(Grid g, ViewArgs a, float* __restr
                     const float cy = __fdiv_rn(__fadd_rn(pv, vc), 2.0f);
                     const float cz = __fdiv_rn(__fadd_rn(pw, wc), 2.0f);
                     const float d = __fadd_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)), __fmul_rn(cz, cz));
-                    ramp_color(R_VEL, __fsqrt_rn(d), col);
+                    ramp_color(ramps, R_VEL, __fsqrt_rn(d), col);
                     break;
                 }
-                case SKT_PRESSURE: ramp_color(R_PRESS, a.p[c], col); break;
+                case SKT_PRESSURE: ramp_color(ramps, R_PRESS, a.p[c], col); break;
                 case SKT_DEBUG1: {  // the "realistic" view of all condensate; faint cells are not drawn
                     const float s = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(a.qw[c], a.qc[c]), a.qr[c]), a.qs[c]), a.qi[c]);
-                    ramp_color(R_REAL, s, col);
+                    ramp_color(ramps, R_REAL, s, col);
                     if ((double)s < 0.0001) {  // float against a double literal, as in the reference
                         k = 0;
                         col[0] = col[1] = col[2] = 0.0f;
@@ -156,7 +166,7 @@ __global__ void __launch_bounds__(256) k_view(Grid g, ViewArgs a, float* __restr
                     break;
                 }
                 case SKT_DEBUG2:
-                case SKT_DEBUG3: ramp_color(R_DEBUG, a.dbg[c], col); break;
+                case SKT_DEBUG3: ramp_color(ramps, R_DEBUG, a.dbg[c], col); break;
                 default: k = 0; break;
             }
         }
@@ -193,40 +203,57 @@ __global__ void __launch_bounds__(256) k_brick_flag(Grid g, BrickGrid b, const f
     }
 }
 
-// exclusive scan of the flags into output slots (one block; the count goes to *count)
-__global__ void __launch_bounds__(1024) k_brick_scan(int nb, int* __restrict__ flags, int* __restrict__ count) {
-    __shared__ int warp_sums[32];
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
+// exclusive scan of the flags into output slots, in two levels: k_brick_scan_blocks scans each
+// run of 1024 flags in one block (slots within the run; the run's total to totals[run]),
+// k_brick_scan_totals scans the run totals into run offsets (one block; *count = all bricks)
+__device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int& total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
     __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int base = 0; base < nb; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const int f = i < nb ? flags[i] : 0;
-        int incl = f;
+    if (wid == 0) {
+        const int ws = lane < nw ? warp_sums[lane] : 0;
+        int wi = ws;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+            const int t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
         }
-        if (lane == 31) warp_sums[wid] = incl;
-        __syncthreads();
-        if (wid == 0) {
-            int ws = warp_sums[lane];
-            int wi = ws;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, wi, o);
-                if (lane >= o) wi += t;
-            }
-            warp_sums[lane] = wi - ws;  // exclusive prefix of the warp totals
-        }
-        __syncthreads();
-        const int slot = carry + warp_sums[wid] + incl - f;
-        if (i < nb) flags[i] = f ? slot : -1;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = slot + f;
-        __syncthreads();
+        if (lane < nw) warp_sums[lane] = wi - ws;
+        if (lane == 31) warp_sums[32] = wi;
+    }
+    __syncthreads();
+    total = warp_sums[32];
+    const int r = warp_sums[wid] + incl - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_brick_scan_blocks(int nb, int* __restrict__ flags, int* __restrict__ totals) {
+    __shared__ int warp_sums[33];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const int f = i < nb ? flags[i] : 0;
+    int total;
+    const int slot = block_exclusive_scan(f, warp_sums, total);
+    if (i < nb) flags[i] = f ? slot : -1;
+    if (threadIdx.x == 0) totals[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_brick_scan_totals(int nruns, int* __restrict__ totals, int* __restrict__ count) {
+    __shared__ int warp_sums[33];
+    int carry = 0;
+    for (int base = 0; base < nruns; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < nruns ? totals[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, warp_sums, total);
+        if (i < nruns) totals[i] = carry + ex;
+        carry += total;
     }
     if (threadIdx.x == 0) *count = carry;
 }
@@ -235,12 +262,13 @@ __global__ void __launch_bounds__(1024) k_brick_scan(int nb, int* __restrict__ f
 // the background; coordinates as three uint32
 template <typename T>
 __global__ void __launch_bounds__(256) k_brick_pack(Grid g, BrickGrid b, const float* __restrict__ f, float bg,
-                                                    const int* __restrict__ slots, T* __restrict__ out,
-                                                    uint32_t* __restrict__ coords) {
+                                                    const int* __restrict__ slots, const int* __restrict__ run_offsets,
+                                                    T* __restrict__ out, uint32_t* __restrict__ coords) {
     const int lane = threadIdx.x & 31;
     for (int br = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; br < b.nb; br += (gridDim.x * blockDim.x) >> 5) {
-        const int slot = slots[br];
+        int slot = slots[br];
         if (slot < 0) continue;
+        slot += run_offsets[br >> 10];
         const int bx = br % b.nbx, by = (br / b.nbx) % b.nby, bz = br / (b.nbx * b.nby);
         T* dst = out + (size_t)slot * kBrickCells;
         for (int k = lane; k < kBrickCells; k += 32) {
@@ -311,7 +339,9 @@ skt_status skt_view_volume(skt_env* env, int sky_param, int ground_param, const 
     cudaMemcpyToSymbolAsync(c_ramps, kRamps, sizeof(kRamps), 0, cudaMemcpyHostToDevice, e.stream);
     float* d_rgb = (float*)e.brick_out;
     uint8_t* d_kind = (uint8_t*)e.brick_out + bytes_rgb;
-    k_view<<<grid_blocks(e, e.g.N), 256, 0, e.stream>>>(e.g, a, d_rgb, d_kind);
+    const int vx = (e.g.X + 127) / 128;
+    const int vz = std::max(1, std::min(e.g.Z, (e.num_sms * 64 + vx * e.g.Y - 1) / (vx * e.g.Y)));  // ~64 blocks per SM
+    k_view<<<dim3(vx, e.g.Y, vz), 128, 0, e.stream>>>(e.g, a, d_rgb, d_kind);
     e.launches += 1;
     cudaMemcpyAsync(rgb, d_rgb, bytes_rgb, cudaMemcpyDeviceToHost, e.stream);
     cudaMemcpyAsync(kind, d_kind, bytes_kind, cudaMemcpyDeviceToHost, e.stream);
@@ -328,18 +358,21 @@ skt_status skt_export_bricks(skt_env* env, int param, int dir, float background,
     if (!f) return report(&e, SKT_INVALID_ARG, "unknown field selector (debug fields need skt_set_diagnostics)");
     BrickGrid b{(e.g.X + kBrick - 1) / kBrick, (e.g.Y + kBrick - 1) / kBrick, (e.g.Z + kBrick - 1) / kBrick, 0};
     b.nb = b.nbx * b.nby * b.nbz;
-    if (!e.brick_flags) {
-        if (cudaMalloc(&e.brick_flags, sizeof(int) * ((size_t)b.nb + 1)) != cudaSuccess) {
+    const int nruns = (b.nb + 1023) / 1024;
+    if (!e.brick_flags) {  // flags, the run totals/offsets, the count
+        if (cudaMalloc(&e.brick_flags, sizeof(int) * ((size_t)b.nb + nruns + 1)) != cudaSuccess) {
             cudaGetLastError();
             e.brick_flags = nullptr;
             return report(&e, SKT_OUT_OF_MEMORY, "brick flag allocation failed");
         }
-        e.brick_count = e.brick_flags + b.nb;
+        e.brick_count = e.brick_flags + b.nb + nruns;
     }
+    int* runs = e.brick_flags + b.nb;
     const int nblk = grid_blocks(e, (long long)b.nb * 32);
     k_brick_flag<<<nblk, 256, 0, e.stream>>>(e.g, b, f, background, threshold, e.brick_flags);
-    k_brick_scan<<<1, 1024, 0, e.stream>>>(b.nb, e.brick_flags, e.brick_count);
-    e.launches += 2;
+    k_brick_scan_blocks<<<nruns, 1024, 0, e.stream>>>(b.nb, e.brick_flags, runs);
+    k_brick_scan_totals<<<1, 1024, 0, e.stream>>>(nruns, runs, e.brick_count);
+    e.launches += 3;
     int n = 0;
     cudaMemcpyAsync(&n, e.brick_count, sizeof(int), cudaMemcpyDeviceToHost, e.stream);
     cudaStreamSynchronize(e.stream);
@@ -361,9 +394,9 @@ skt_status skt_export_bricks(skt_env* env, int param, int dir, float background,
     }
     uint32_t* d_coords = (uint32_t*)((char*)e.brick_out + vbytes);
     if (half)
-        k_brick_pack<__half><<<nblk, 256, 0, e.stream>>>(e.g, b, f, background, e.brick_flags, (__half*)e.brick_out, d_coords);
+        k_brick_pack<__half><<<nblk, 256, 0, e.stream>>>(e.g, b, f, background, e.brick_flags, runs, (__half*)e.brick_out, d_coords);
     else
-        k_brick_pack<float><<<nblk, 256, 0, e.stream>>>(e.g, b, f, background, e.brick_flags, (float*)e.brick_out, d_coords);
+        k_brick_pack<float><<<nblk, 256, 0, e.stream>>>(e.g, b, f, background, e.brick_flags, runs, (float*)e.brick_out, d_coords);
     e.launches += 1;
     cudaMemcpyAsync(values, e.brick_out, vbytes, cudaMemcpyDeviceToHost, e.stream);
     cudaMemcpyAsync(coords, d_coords, cbytes, cudaMemcpyDeviceToHost, e.stream);

@@ -237,7 +237,7 @@ __device__ __forceinline__ float ppm_cdt(const Grid& g, float dtFull, int nsub, 
 // previous warp's cells: its flux (and q(x0-1)) is computed for 32 planes at once, one plane per
 // lane, and handed to lane 0 plane by plane, so the warp does not spend a whole flux evaluation
 // per plane on one lane.
-__global__ void __launch_bounds__(32 * DVY) k_ppm4x(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
+__global__ void __launch_bounds__(32 * DVY, 8) k_ppm4x(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
                                                     const float* __restrict__ vel, const float* __restrict__ def, int sides,
                                                     const float* __restrict__ defU, float dtFull, int nsub_host, int half,
                                                     const Scalars* __restrict__ sc, int slot) {
