@@ -120,19 +120,20 @@ skt_status run_step(Env& e, float dt, float speed) {
     // moisture
     launch_diffuse(e, e.qv, 1, dtS);
     e.last_nsub[4] = launch_advect(e, e.qv, e.isenQv, CUSTOM, CUSTOM, dtS, 4, hs);
+    // the wind is the same for every moisture field: its substep count is computed once
     launch_diffuse(e, e.qw, 5, dtS);
-    e.last_nsub[5] = launch_advect(e, e.qw, e.zeroY, DIRICHLET, DIRICHLET, dtS, 5, hs);
+    e.last_nsub[5] = launch_advect(e, e.qw, e.zeroY, DIRICHLET, DIRICHLET, dtS, 5, hs, true);
     launch_diffuse(e, e.qc, 5, dtS);
-    e.last_nsub[6] = launch_advect(e, e.qc, e.zeroY, DIRICHLET, DIRICHLET, dtS, 6, hs);
+    e.last_nsub[6] = launch_advect(e, e.qc, e.zeroY, DIRICHLET, DIRICHLET, dtS, 6, hs, true);
     // rain, snow and ice: diffuse, fall, advect each (the reference's order per species; the
     // species do not read one another here, so the three falls run as one column march)
     launch_diffuse(e, e.qr, 5, dtS);
     launch_diffuse(e, e.qs, 5, dtS);
     launch_diffuse(e, e.qi, 5, dtS);
     launch_precip3(e, dtS);
-    e.last_nsub[7] = launch_advect(e, e.qr, e.zeroY, DIRICHLET, DIRICHLET, dtS, 7, hs);
-    e.last_nsub[8] = launch_advect(e, e.qs, e.zeroY, DIRICHLET, DIRICHLET, dtS, 8, hs);
-    e.last_nsub[9] = launch_advect(e, e.qi, e.zeroY, DIRICHLET, DIRICHLET, dtS, 9, hs);
+    e.last_nsub[7] = launch_advect(e, e.qr, e.zeroY, DIRICHLET, DIRICHLET, dtS, 7, hs, true);
+    e.last_nsub[8] = launch_advect(e, e.qs, e.zeroY, DIRICHLET, DIRICHLET, dtS, 8, hs, true);
+    e.last_nsub[9] = launch_advect(e, e.qi, e.zeroY, DIRICHLET, DIRICHLET, dtS, 9, hs, true);
     // microphysics + latent heat
     launch_micro(e, dt, speed);
     // clock (m_time, Game/environment.cu:550-551)

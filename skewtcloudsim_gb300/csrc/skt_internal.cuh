@@ -130,6 +130,7 @@ struct Env {
     float *isenT, *isenQv, *defU, *defW, *zeroY;
     float* pcol = nullptr;        // the init's pressure column (the editor's pressure reset)
     int ground_changed = 0;       // the ground changed since the last step (m_groundChanged)
+    int adv_nsub = -1;            // Courant substeps of the last advection's wind (host copy; 0 = on the device only)
     // reductions
     Scalars* sc;
     double* partials;
@@ -202,7 +203,8 @@ struct ProfScope {
 
 // ---- launchers (defined in the kernel translation units) --------------------------------------
 void launch_diffuse(Env& e, float* f, int type, float dtS);
-int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int field_slot, bool host_sync);
+int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int field_slot, bool host_sync,
+                  bool same_wind = false);
 void launch_precip(Env& e, float* q, int type, float dtS);
 void launch_precip3(Env& e, float dtS);  // rain, snow and ice in one column march
 void launch_buoyancy(Env& e, float dtS);

@@ -829,27 +829,38 @@ void launch_diffuse(Env& e, float* f, int type, float dtS) {
 // advectPPMWGPU Game/environment.cu:692-824. With host_sync the substep count is read back as
 // the reference does; otherwise max_substeps slots are launched and the ones beyond the device
 // count exit at once (graph capture). Returns the substep count (or -1 when not read back).
-int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int slot_id, bool host_sync) {
+int launch_advect(Env& e, float* f, const float* def, int sides, int ground, float dtS, int slot_id, bool host_sync,
+                  bool same_wind) {
     const Grid& g = e.g;
     ProfScope ps(e, "advect");
-    e.launches += 2;
-    cudaMemsetAsync(&e.sc->maxbits, 0, sizeof(unsigned int), e.stream);
-    if (e.flat && (g.X % 4) == 0) {
-        const int n4 = g.N / 4;
-        k_maxvel4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, g.XY / 4, (const float4*)e.u,
-                                                                                  (const float4*)e.v, (const float4*)e.w,
-                                                                                  e.cfg.semantics == 0, e.sc);
-    } else {
-        k_maxvel<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, e.u, e.v, e.w, e.cfg.semantics == 0, e.sc);
+    // same_wind: the wind has not changed since the last advection (the moisture fields after the
+    // projection), so its Courant substep count (sc->nsub, and the host copy) stands
+    if (!same_wind || e.adv_nsub < 0) {
+        e.launches += 2;
+        cudaMemsetAsync(&e.sc->maxbits, 0, sizeof(unsigned int), e.stream);
+        if (e.flat && (g.X % 4) == 0) {
+            const int n4 = g.N / 4;
+            k_maxvel4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, g.XY / 4, (const float4*)e.u,
+                                                                                      (const float4*)e.v, (const float4*)e.w,
+                                                                                      e.cfg.semantics == 0, e.sc);
+        } else {
+            k_maxvel<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, e.u, e.v, e.w, e.cfg.semantics == 0, e.sc);
+        }
+        k_nsub<<<1, 1, 0, e.stream>>>(e.sc, dtS, g.vox, float(e.cfg.max_substeps));
+        e.adv_nsub = -1;
+        if (host_sync) {
+            cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
+            cudaStreamSynchronize(e.stream);
+            e.adv_nsub = e.host_sc->nsub;
+        } else {
+            e.adv_nsub = 0;  // on the device only (sc->nsub)
+        }
     }
-    k_nsub<<<1, 1, 0, e.stream>>>(e.sc, dtS, g.vox, float(e.cfg.max_substeps));
     int nsub = -1;
     int slots;
     const Scalars* chk = nullptr;
     if (host_sync) {
-        cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-        cudaStreamSynchronize(e.stream);
-        nsub = e.host_sc->nsub;
+        nsub = e.adv_nsub;
         slots = nsub;
     } else {
         slots = e.cfg.max_substeps;
@@ -879,6 +890,18 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     const int ncopy = std::min((n4 + 255) / 256, e.num_sms * 8);
     e.launches += 6LL * slots;
     for (int i = 0; i < slots; ++i) {
+        if (vec && f != e.v) {
+            // A -> O -> B -> O -> B -> A through the second scratch field: the last pass writes the
+            // field's sky cells itself (no copy). A pass reads the wind as it stands: for u (x
+            // passes) and w (z pass) that is the chain's current buffer.
+            float* B = e.tB;
+            k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
+            k_ppm4y<<<yg, yb, 0, e.stream>>>(g, ylen, O, B, e.v, def, sides, ground, dtS, nsub, 1, chk, i);
+            k_ppm4z<<<vg2, vb, 0, e.stream>>>(g, zlen2, B, O, f == e.w ? B : e.w, def, sides, e.defW, dtS, nsub, 0, chk, i);
+            k_ppm4y<<<yg, yb, 0, e.stream>>>(g, ylen, O, B, e.v, def, sides, ground, dtS, nsub, 1, chk, i);
+            k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, B, A, f == e.u ? B : e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
+            continue;
+        }
         if (vec) {
             k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
             const float* vy = e.v;
