@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(RT) k_update_mg(int n, const float* __restrict
 
 // ---- vector levels (X % 4 == 0) -------------------------------------------------------------
 
-constexpr int JVY = 4;
+constexpr int JVY = 8;  // rows per block: the rows above and below come mostly from L1
 
 // The vector levels (X % 4 == 0) run every V-cycle step as one float4 z march: a thread owns
 // four consecutive x cells of one (y) row and walks a run of z planes, keeping the input vector
@@ -605,7 +605,7 @@ struct Stencil4 {
 // being written only). DOT forms z.r (r = b) of the finest level's output for the CG:
 // DOT_START sets sigma0 and restarts the iteration count, DOT_NEXT sets beta = rho_new/rho.
 template <int MODE, int DOT, class CT>
-__global__ void __launch_bounds__(32 * JVY, 8) k_mg_smooth4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
+__global__ void __launch_bounds__(32 * JVY, 32 / JVY) k_mg_smooth4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
                                                          const CT* __restrict__ az, const CT* __restrict__ aw, const float* __restrict__ b,
                                                          UIn<MODE, CT> U, UIn<SM_POSTA, CT> Pv, float* out, float k1, float k2,
                                                          const int* skip, Scalars* sc, double* partials) {
@@ -683,7 +683,7 @@ __global__ void __launch_bounds__(32 * JVY, 8) k_mg_smooth4(int X, int Y, int Z,
 // eight children. zlen, the z offset of every block, Y and JVY are even: a thread sums its row's
 // x pairs over two planes, then the even row of each row pair adds its partner's sums.
 template <class CT>
-__global__ void __launch_bounds__(32 * JVY, 8) k_mg_restrict4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
+__global__ void __launch_bounds__(32 * JVY, 32 / JVY) k_mg_restrict4(int X, int Y, int Z, int zlen, const CT* __restrict__ ax, const CT* __restrict__ ay,
                                                            const CT* __restrict__ az, const CT* __restrict__ aw, const float* __restrict__ x,
                                                            const float* __restrict__ b, int CX, int CY, float* __restrict__ cb, const int* skip) {
     if (skip && *skip) return;
@@ -741,7 +741,7 @@ __global__ void __launch_bounds__(32 * JVY, 8) k_mg_restrict4(int X, int Y, int 
 
 // CG search step fused with the operator: s_new = z + beta s_old (beta = 0: s_new = z, s_old
 // is not read), As = A s_new with the FP32 finest coefficients, s_new.As -> alpha = rho/(s.As)
-__global__ void __launch_bounds__(32 * JVY, 8) k_mg_matvec_search4(int X, int Y, int Z, int zlen, const float* __restrict__ ax,
+__global__ void __launch_bounds__(32 * JVY, 32 / JVY) k_mg_matvec_search4(int X, int Y, int Z, int zlen, const float* __restrict__ ax,
                                                                 const float* __restrict__ ay, const float* __restrict__ az,
                                                                 const float* __restrict__ aw, const float* __restrict__ zv,
                                                                 const float* __restrict__ sold, float* __restrict__ snew,

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(256) k_diffuse(Grid g, const float* __restrict
 // Vectorised sweep for flat terrain (ground = the y = 0 layer) and X % 4 == 0: four cells per
 // thread along x, a march along z holding the planes z-1, z, z+1 in registers, x neighbours from
 // the neighbouring lanes. Same arithmetic and ghost values as k_diffuse.
-constexpr int DVY = 4;
+constexpr int DVY = 16;  // rows per block: the rows above and below come mostly from L1
 __device__ __forceinline__ float4 ld4f(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
 __device__ __forceinline__ float side_val(int bc, float own, float d) { return bc == NEUMANN ? own : (bc == DIRICHLET ? 0.0f : d); }
 
@@ -237,7 +237,7 @@ __device__ __forceinline__ float ppm_cdt(const Grid& g, float dtFull, int nsub, 
 // previous warp's cells: its flux (and q(x0-1)) is computed for 32 planes at once, one plane per
 // lane, and handed to lane 0 plane by plane, so the warp does not spend a whole flux evaluation
 // per plane on one lane.
-__global__ void __launch_bounds__(32 * DVY, 8) k_ppm4x(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
+__global__ void __launch_bounds__(32 * DVY, 32 / DVY) k_ppm4x(Grid g, int zlen, const float* __restrict__ in, float* __restrict__ out,
                                                     const float* __restrict__ vel, const float* __restrict__ def, int sides,
                                                     const float* __restrict__ defU, float dtFull, int nsub_host, int half,
                                                     const Scalars* __restrict__ sc, int slot) {
