@@ -510,6 +510,165 @@ __global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* 
     }
 }
 
+// k_build for flat terrain and X % 4 == 0: four cells per thread, a march along z in blocks of
+// MVY rows. Each cell's reciprocal density is formed once (the x neighbours' by shuffle, the next
+// plane's carried), and each face once: a cell forms its right, up and front faces; the left face
+// is the right face of the cell before (a shuffle across lanes), the back face the front face of
+// the previous plane, the down face is formed again from the row below. coef_of and the harmonic
+// mean are symmetric in their two densities (IEEE addition commutes), so every value equals
+// k_build's; z.r is summed in FP64 in a different order.
+__device__ __forceinline__ float fcomp(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+__device__ __forceinline__ void fset(float4& v, int k, float a) {
+    if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
+}
+__device__ __forceinline__ void face_of(float c, float rc, float n, float rn, float& h, float& coef) {
+    // hm(n) = 2/(1/c + 1/n) and coef_of(c, n) = -max(1, 1.225/hm), both 0 across a zero density
+    if (n == 0.0f) { h = 0.0f; coef = 0.0f; return; }
+    h = 2.0f / (rc + rn);
+    coef = -fmaxf(1.0f, 1.225f / h);
+    (void)c;
+}
+__global__ void __launch_bounds__(MVT) k_build4(Grid g, int zlen, const float* __restrict__ rho, const float* __restrict__ u,
+                                                const float* __restrict__ v, const float* __restrict__ w,
+                                                const float* __restrict__ defU, const float* __restrict__ defW, float dt,
+                                                float* __restrict__ ax, float* __restrict__ ay, float* __restrict__ az,
+                                                float* __restrict__ aw, float* __restrict__ r, float* __restrict__ s,
+                                                float* __restrict__ pp, float* __restrict__ As, int reference, Scalars* sc,
+                                                double* partials) {
+    __shared__ double smd[MVT / 32];
+    __shared__ float smf[MVT / 32];
+    const int lane = threadIdx.x, tid = threadIdx.x + 32 * threadIdx.y;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * MVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const bool sky = act && y >= 1;
+    const int X = g.X, XY = g.XY, Z = g.Z;
+    const int row = x0 + y * X;
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    double dsum = 0.0;
+    float mx = 0.0f;
+    const float du_ = sky ? defU[y] : 0.0f, dw_ = sky ? defW[y] : 0.0f;
+    // own plane: density and reciprocal; the back face (front face of the plane before) and w there
+    float4 pc = z4, rc = z4, hB = z4, cB = z4, wB = z4;
+    if (sky) {
+        pc = ld4(rho, row + zs * XY);
+        rc = make_float4(1.0f / pc.x, 1.0f / pc.y, 1.0f / pc.z, 1.0f / pc.w);
+        float4 pb = pc, rb = rc;  // outside at z = 0: the own density (NEUMANN)
+        if (zs > 0) {
+            pb = ld4(rho, row + (zs - 1) * XY);
+            rb = make_float4(1.0f / pb.x, 1.0f / pb.y, 1.0f / pb.z, 1.0f / pb.w);
+            wB = ld4(w, row + (zs - 1) * XY);
+        } else {
+            wB = make_float4(dw_, dw_, dw_, dw_);
+        }
+        face_of(pc.x, rc.x, pb.x, rb.x, hB.x, cB.x);
+        face_of(pc.y, rc.y, pb.y, rb.y, hB.y, cB.y);
+        face_of(pc.z, rc.z, pb.z, rb.z, hB.z, cB.z);
+        face_of(pc.w, rc.w, pb.w, rb.w, hB.w, cB.w);
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 pf = pc, rf = rc, pd = z4, rd = z4, pu = pc, ru = rc, uo = z4, vo = z4, wo = z4, vd = z4;
+        if (sky) {
+            if (z + 1 < Z) {
+                pf = ld4(rho, c + XY);
+                rf = make_float4(1.0f / pf.x, 1.0f / pf.y, 1.0f / pf.z, 1.0f / pf.w);
+            }
+            if (y > 1) {  // the row below (y = 1 has the ground below: density 0, v 0)
+                pd = ld4(rho, c - X);
+                rd = make_float4(1.0f / pd.x, 1.0f / pd.y, 1.0f / pd.z, 1.0f / pd.w);
+                vd = ld4(v, c - X);
+            }
+            if (y + 1 < g.Y) {
+                pu = ld4(rho, c + X);
+                ru = make_float4(1.0f / pu.x, 1.0f / pu.y, 1.0f / pu.z, 1.0f / pu.w);
+            }
+            uo = ld4(u, c);
+            vo = ld4(v, c);
+            wo = ld4(w, c);
+        }
+        // the right neighbour of the last cell and the left neighbour of the first
+        float pr = __shfl_down_sync(0xffffffffu, pc.x, 1), rr = __shfl_down_sync(0xffffffffu, rc.x, 1);
+        float ul = __shfl_up_sync(0xffffffffu, uo.w, 1);
+        if (sky && (lane == 31 || x0 + 4 >= X)) {
+            if (x0 + 4 < X) { pr = rho[c + 4]; rr = 1.0f / pr; }
+            else { pr = pc.w; rr = rc.w; }  // outside: the own density (NEUMANN)
+        }
+        float hR[4], cR[4];
+        face_of(pc.x, rc.x, pc.y, rc.y, hR[0], cR[0]);
+        face_of(pc.y, rc.y, pc.z, rc.z, hR[1], cR[1]);
+        face_of(pc.z, rc.z, pc.w, rc.w, hR[2], cR[2]);
+        face_of(pc.w, rc.w, pr, rr, hR[3], cR[3]);
+        float hL0 = __shfl_up_sync(0xffffffffu, hR[3], 1), cL0 = __shfl_up_sync(0xffffffffu, cR[3], 1);
+        if (sky && lane == 0) {
+            float pl = pc.x, rl = rc.x;
+            if (x0 > 0) { pl = rho[c - 1]; rl = 1.0f / pl; ul = u[c - 1]; }
+            else ul = du_;
+            face_of(pc.x, rc.x, pl, rl, hL0, cL0);
+        }
+        if (sky) {
+            const float hL[4] = {hL0, hR[0], hR[1], hR[2]}, cL[4] = {cL0, cR[0], cR[1], cR[2]};
+            const float uL[4] = {ul, uo.x, uo.y, uo.z};
+            float4 oax, oay, oaz, oaw, orr, oss;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float cur = fcomp(pc, k);
+                float hU, cU, hD, cD, hF, cF;
+                face_of(cur, fcomp(rc, k), fcomp(pu, k), fcomp(ru, k), hU, cU);
+                face_of(cur, fcomp(rc, k), fcomp(pd, k), fcomp(rd, k), hD, cD);
+                face_of(cur, fcomp(rc, k), fcomp(pf, k), fcomp(rf, k), hF, cF);
+                float wd = 0.0f;
+                wd -= cR[k]; wd -= cL[k]; wd -= cU; wd -= cD; wd -= cF; wd -= fcomp(cB, k);
+                const float mfd = ((hR[k] * fcomp(uo, k) - hL[k] * uL[k]) + (hU * fcomp(vo, k) - hD * fcomp(vd, k)) +
+                                   (hF * fcomp(wo, k) - fcomp(hB, k) * fcomp(wB, k)));
+                const float dch = (cur - cur) / dt;  // the reference's old density is a copy of rho
+                const float rv = mfd - dch;
+                const float zv = rv * precon_of(wd);
+                fset(oax, k, cR[k]); fset(oay, k, cU); fset(oaz, k, cF); fset(oaw, k, wd);
+                fset(orr, k, rv); fset(oss, k, zv);
+                dsum += double(zv) * double(rv);
+                const float m = (!reference || z == 0) ? fabsf(rv) : rv;
+                if (m > mx) mx = m;
+                fset(hB, k, hF); fset(cB, k, cF);
+            }
+            *reinterpret_cast<float4*>(ax + c) = oax;
+            *reinterpret_cast<float4*>(ay + c) = oay;
+            *reinterpret_cast<float4*>(az + c) = oaz;
+            *reinterpret_cast<float4*>(aw + c) = oaw;
+            *reinterpret_cast<float4*>(r + c) = orr;
+            *reinterpret_cast<float4*>(s + c) = oss;
+            *reinterpret_cast<float4*>(pp + c) = z4;
+            *reinterpret_cast<float4*>(As + c) = z4;
+        } else if (act) {  // the ground row
+            *reinterpret_cast<float4*>(ax + c) = z4;
+            *reinterpret_cast<float4*>(ay + c) = z4;
+            *reinterpret_cast<float4*>(az + c) = z4;
+            *reinterpret_cast<float4*>(aw + c) = z4;
+            *reinterpret_cast<float4*>(r + c) = z4;
+            *reinterpret_cast<float4*>(s + c) = z4;
+            *reinterpret_cast<float4*>(pp + c) = z4;
+            *reinterpret_cast<float4*>(As + c) = z4;
+        }
+        pc = pf;
+        rc = rf;
+        wB = wo;
+    }
+    const double bs = block_sum_n<MVT>(dsum, smd, tid);
+    const float bm = block_max_n<MVT>(mx, smf, tid);
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    double tot;
+    float mall;
+    if (publish_n<MVT>(sc, partials, bid, nb, tid, bs, bm, tot, mall)) {
+        sc->sigma0 = tot;
+        sc->sigma1 = 0.0;
+        sc->iters = 0;
+        sc->residual = mall;
+        sc->converged = (mall == 0.0f) ? 1 : 0;
+    }
+}
+
 // updatePressure (:1016-1030) followed by initDensity (:1432-1452)
 __global__ void __launch_bounds__(256) k_press_dens(Grid g, float* __restrict__ p, const float* __restrict__ pp, float* __restrict__ rho,
                                                     const float* __restrict__ th, const float* __restrict__ qv, const float* __restrict__ Pg) {
@@ -574,8 +733,18 @@ void launch_project(Env& e, float dtS) {
     ProfScope ps(e, "proj_setup");
     e.launches += 2;
     k_reset_vel<<<(g.XY + 127) / 128, 128, 0, e.stream>>>(g, e.u, e.v, e.w, e.defU, e.defW, ref);
-    k_build<<<nblk, NT, 0, e.stream>>>(g, T, e.rho, e.u, e.v, e.w, e.defU, e.defW, dtS, e.ax, e.ay, e.az, e.aw, e.r, e.s, e.pp, e.As, ref,
-                                      e.sc, e.partials);
+    if (e.flat && (g.X % 4) == 0) {
+        const int gx = (g.X / 4 + 31) / 32, gy = (g.Y + MVY - 1) / MVY;
+        int zc = std::max(1, std::min(g.Z, (e.num_sms * 4 + gx * gy - 1) / (gx * gy)));
+        while (gx * gy * zc > kMaxPartials && zc > 1) --zc;
+        const int zlen = (g.Z + zc - 1) / zc;
+        zc = (g.Z + zlen - 1) / zlen;
+        k_build4<<<dim3(gx, gy, zc), dim3(32, MVY), 0, e.stream>>>(g, zlen, e.rho, e.u, e.v, e.w, e.defU, e.defW, dtS, e.ax, e.ay, e.az,
+                                                                   e.aw, e.r, e.s, e.pp, e.As, ref, e.sc, e.partials);
+    } else {
+        k_build<<<nblk, NT, 0, e.stream>>>(g, T, e.rho, e.u, e.v, e.w, e.defU, e.defW, dtS, e.ax, e.ay, e.az, e.aw, e.r, e.s, e.pp, e.As,
+                                          ref, e.sc, e.partials);
+    }
     }
     if (e.cfg.precision == 1) {
         mg_solve(e);
