@@ -253,6 +253,62 @@ def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
             "outer": sd.get("outer_iters", 0), "converged": sd["converged"], "residual": sd["pcg_residual"]}
 
 
+def run_ensemble(args, rank, world, local, pg, torch):
+    """The batched ensemble (``--workload ensemble-48``): 48 members of uneven sizes drawn from
+    {64x64x32, 96x96x64, 128x128x64, 192x192x96}, each with its own seeded sounding and bubble, all
+    advanced together by skt_step_ensemble (a host thread per member, each member on its own
+    stream), mixed precision unless ``--mode plain``. Metric: members x cell-steps/s over the whole
+    job (host wall clock around the timed steps with a device synchronise on both sides)."""
+    from skewtcloudsim_gb300 import Environment, SolverConfig, sounding, step_ensemble
+    n = int(args.workload.split("-")[1])
+    members = sounding.ensemble_members(n, seed=4000 + 1000 * rank)
+    prec = 0 if args.mode == "plain" else 1
+    envs = []
+    for st, dt, speed in members:
+        env = Environment(st.nx, st.ny, st.nz, st.voxel, SolverConfig(semantics=0 if prec == 0 else 1, precision=prec))
+        env.init_from(st)
+        envs.append(env)
+    dts = [m[1] for m in members]
+    cells = sum(m[0].n for m in members)
+    step_ensemble(envs, dts, 1.0, nsteps=args.warmup)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    l0 = sum(e.stats()["kernel_launches"] for e in envs)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        step_ensemble(envs, dts, 1.0, nsteps=args.steps)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+    launches = sum(e.stats()["kernel_launches"] for e in envs) - l0
+    el = t1 - t0
+    if pg:
+        t = torch.tensor([el], device="cuda")
+        pg.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el = float(t.item())
+    # one sequential pass for comparison: the same members stepped one after another
+    torch.cuda.synchronize()
+    s0 = time.perf_counter()
+    for env, dt in zip(envs, dts):
+        env.update_gpu(dt, 1.0, nsteps=1)
+    torch.cuda.synchronize()
+    seq = time.perf_counter() - s0
+    for env in envs:
+        env.close()
+    if rank == 0:
+        value = cells * args.steps * world / el
+        print(json.dumps({
+            "metric": f"members x cell-steps/s, ensemble of {n} uneven members", "value": value, "unit": "cell-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "members": n, "cells": cells, "pcg": "mixed" if prec else "plain",
+                       "sizes": sorted({f"{m[0].nx}x{m[0].nz}x{m[0].ny}" for m in members}),
+                       "concurrency": "one host thread per member, one stream per member",
+                       "sequential_ms_per_step": seq * 1e3, "parallelism": "single" if world == 1 else f"replicas{world}"},
+            "gpu_launches": launches, "clocks": clk.summary()}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -281,6 +337,8 @@ def main():
         pg = dist
     from skewtcloudsim_gb300 import Environment, SolverConfig, sounding, build
     build.build()
+    if args.workload.startswith("ensemble-"):
+        return run_ensemble(args, rank, world, local, pg, torch)
 
     shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
     init, dt, speed = sounding.workload(args.workload, scale=shape)

@@ -124,6 +124,16 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps);
 /* Waits for the environment's stream. */
 skt_status skt_sync(skt_env* env);
 
+/* Ensemble stepping: advances n independent environments (members of any grid sizes, each with
+ * its own state) by nsteps steps each. Every member already runs on its own CUDA stream; here up
+ * to `threads` host threads (0: one per member, at most 64) drive the members' steps at once, so
+ * the kernels of small members run side by side on the GPU instead of one member after another.
+ * dt and speed hold one value per member (NULL: dt0 / 1 for all). Returns SKT_OK, or the first
+ * failing member's status (SKT_NOT_CONVERGED counts as OK, as for skt_step); statuses, when not
+ * NULL, receives every member's own status. Results equal stepping the members one by one. */
+skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float dt0, const float* speed, int nsteps,
+                             int threads, int* statuses);
+
 /* Field readback: the per-field copies of editor::GPUSetEnv (Game/editor.cpp:226-260).
  * dir selects the wind component for SKT_WIND. n must equal nx*ny*nz. Synchronous. */
 skt_status skt_read_field(skt_env* env, int param, int dir, float* host_dst, size_t n);

@@ -7,7 +7,10 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 using namespace skt;
@@ -413,6 +416,39 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
         return fail(&e, skt_status(dev_status), "a kernel gave up waiting for its streamed data (device-side wait limit)");
     }
     return worst;
+}
+
+skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float dt0, const float* speed, int nsteps,
+                             int threads, int* statuses) {
+    if (!envs || n < 0 || nsteps < 0) return fail(nullptr, SKT_INVALID_ARG, "invalid ensemble arguments");
+    for (int i = 0; i < n; ++i)
+        if (!envs[i]) return fail(nullptr, SKT_INVALID_ARG, "null member");
+    if (n == 0) return SKT_OK;
+    int device = 0;
+    cudaGetDevice(&device);
+    const int nt = std::min(n, threads > 0 ? threads : std::min(n, 64));
+    std::vector<int> st(n, SKT_OK);
+    std::atomic<int> next(0);
+    auto work = [&]() {
+        cudaSetDevice(device);  // the calling thread's device, for every worker
+        for (int i = next++; i < n; i = next++)
+            st[i] = skt_step(envs[i], dt ? dt[i] : dt0, speed ? speed[i] : 1.0f, nsteps);
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    skt_status first = SKT_OK;
+    for (int i = 0; i < n; ++i) {
+        if (statuses) statuses[i] = st[i];
+        if (first == SKT_OK && st[i] != SKT_OK && st[i] != SKT_NOT_CONVERGED) first = skt_status(st[i]);
+    }
+    if (first != SKT_OK) {
+        for (int i = 0; i < n; ++i)
+            if (st[i] == first) { g_create_err = "member " + std::to_string(i) + ": " + envs[i]->e.err; break; }
+    }
+    return first;
 }
 
 skt_status skt_sync(skt_env* env) {

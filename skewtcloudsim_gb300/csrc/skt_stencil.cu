@@ -714,6 +714,144 @@ __global__ void __launch_bounds__(256) k_buoyancy(Grid g, float* __restrict__ v,
     v[c] = vel + change;
 }
 
+// k_buoyancy for flat terrain and X % 4 == 0: four cells per thread and a march up the rows. A
+// cell's temperature th (p/Pg)^kappa and its ws(T - 273.15, p) are the "down" values of the cell
+// above and the "up" values of the cell below (the same calls on the same inputs), so each is
+// formed once per cell and handed along the march instead of three times. The horizontal means
+// take x neighbours from the neighbouring lanes and z neighbours from the rows of the block's
+// other warps. Arithmetic and the order of every sum as in k_buoyancy.
+constexpr int BZ4 = 8;
+__device__ __forceinline__ float buoy_change(float vel, bool up, bool down, float Pgs, float psC, float psU, float psD, float QP,
+                                             float Qenv, float QenvUp, float QenvDown, float thc, float thU, float thD, float Tc,
+                                             float TUp, float TDown, float WUp, float WDown, float Tenv, float totalQ, float dt) {
+    float Tad = thc, TadUp = thc, TadDown = thc;
+    const float TenvUp = thU, TenvDown = thD;
+    if (down) {
+        if ((Tc < 0.0f && QP >= wi(TDown - 273.15f, psD)) || QP >= WDown) {
+            TadDown = Tc - MLR(Tc - 273.15f, psC) * (psC - psD);
+            TadDown = TadDown * powf(Pgs / psD, KC::KAPPA);
+        }
+    }
+    if (up) {
+        if ((Tc < 0.0f && QP >= wi(TUp - 273.15f, psU)) || QP >= WUp) {
+            TadUp = MLR(Tc - 273.15f, psC) * (psU - psC) + Tc;
+            TadUp = TadUp * powf(Pgs / psU, KC::KAPPA);
+        }
+    }
+    float B = 0.0f, BUp = 0.0f, BDown = 0.0f;
+    if (down) {
+        const float VTP = TadDown * (1.0f + 0.608f * QP), VTE = TenvDown * (1.0f + 0.608f * QenvDown);
+        BDown = KC::g * ((VTP - VTE) / VTE) - totalQ * KC::g;
+    }
+    {
+        const float VTP = Tad * (1.0f + 0.608f * QP), VTE = Tenv * (1.0f + 0.608f * Qenv);
+        B = KC::g * ((VTP - VTE) / VTE) - totalQ * KC::g;
+    }
+    if (up) {
+        const float VTP = TadUp * (1.0f + 0.608f * QP), VTE = TenvUp * (1.0f + 0.608f * QenvUp);
+        BUp = KC::g * ((VTP - VTE) / VTE) - totalQ * KC::g;
+    }
+    float fin = B;
+    if (vel > 0.0f) fin = BUp;
+    else if (vel < 0.0f) fin = BDown;
+    float change = fin * dt;
+    if ((up && vel > 0.0f && -change > vel) || (down && vel < 0.0f && -change < vel)) change = -vel;
+    return change;
+}
+
+__global__ void __launch_bounds__(32 * BZ4) k_buoyancy4(Grid g, int ylen, float* __restrict__ v, const float* __restrict__ th,
+                                                        const float* __restrict__ qv, const float* __restrict__ qr,
+                                                        const float* __restrict__ qs, const float* __restrict__ qi,
+                                                        const float* __restrict__ p, const float* __restrict__ Pg, float dt,
+                                                        float* __restrict__ dbg) {
+    const int lane = threadIdx.x;
+    const int xw = blockIdx.x * 128, x0 = xw + lane * 4;
+    const int z = blockIdx.y * BZ4 + threadIdx.y;
+    const int ys = 1 + blockIdx.z * ylen, ye = min(ys + ylen, g.Y);
+    if (xw >= g.X || z >= g.Z || ys >= g.Y) return;  // the whole warp
+    const bool act = x0 < g.X;
+    const int X = g.X, XY = g.XY, Y = g.Y, Z = g.Z;
+    const int col = x0 + z * XY;  // + y*X
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    const float4 pg = act ? ld4f(Pg, x0 + z * X) : make_float4(1, 1, 1, 1);
+    // valid horizontal neighbours per cell (flat terrain: the in-domain ones)
+    float nv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = x0 + k;
+        nv[k] = float(int(x + 1 < X) + int(x > 0) + int(z + 1 < Z) + int(z > 0));
+    }
+    auto temps = [&](const float4& thv, const float4& pv, float4& T, float4& W) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float t = comp(thv, k) * powf(comp(pv, k) / comp(pg, k), KC::KAPPA);
+            setc(T, k, t);
+            setc(W, k, ws(t - 273.15f, comp(pv, k)));
+        }
+    };
+    // rows y-1 (d), y (c), y+1 (u): theta, qv, p, T, W
+    float4 thd = z4, qvd = z4, pd = z4, Td = z4, Wd = z4;
+    float4 thc = z4, qvc = z4, pc = z4, Tc = z4, Wc = z4;
+    if (act) {
+        if (ys >= 2) {
+            const int c = col + (ys - 1) * X;
+            thd = ld4f(th, c); qvd = ld4f(qv, c); pd = ld4f(p, c);
+            temps(thd, pd, Td, Wd);
+        }
+        const int c = col + ys * X;
+        thc = ld4f(th, c); qvc = ld4f(qv, c); pc = ld4f(p, c);
+        temps(thc, pc, Tc, Wc);
+    }
+    for (int y = ys; y < ye; ++y) {
+        const int c = col + y * X;
+        const bool up = y < Y - 1, down = y >= 2;
+        float4 thu = z4, qvu = z4, pu = pc, Tu = z4, Wu = z4;
+        float4 vel = z4, tq = z4, thb = z4, thf = z4, qb = z4, qf = z4;
+        if (act) {
+            if (up) {
+                thu = ld4f(th, c + X); qvu = ld4f(qv, c + X); pu = ld4f(p, c + X);
+                temps(thu, pu, Tu, Wu);
+            }
+            vel = ld4f(v, c);
+            const float4 a = ld4f(qr, c), b = ld4f(qs, c), d = ld4f(qi, c);
+            tq = make_float4(a.x + b.x + d.x, a.y + b.y + d.y, a.z + b.z + d.z, a.w + b.w + d.w);
+            if (z > 0) { thb = ld4f(th, c - XY); qb = ld4f(qv, c - XY); }
+            if (z + 1 < Z) { thf = ld4f(th, c + XY); qf = ld4f(qv, c + XY); }
+        }
+        // x neighbours of the row's ends (outside the domain: DIRICHLET, 0)
+        float thl = __shfl_up_sync(0xffffffffu, thc.w, 1), ql = __shfl_up_sync(0xffffffffu, qvc.w, 1);
+        float thr = __shfl_down_sync(0xffffffffu, thc.x, 1), qr_ = __shfl_down_sync(0xffffffffu, qvc.x, 1);
+        if (act) {
+            if (lane == 0) { thl = x0 > 0 ? th[c - 1] : 0.0f; ql = x0 > 0 ? qv[c - 1] : 0.0f; }
+            if (lane == 31 || x0 + 4 >= X) {
+                thr = x0 + 4 < X ? th[c + 4] : 0.0f;
+                qr_ = x0 + 4 < X ? qv[c + 4] : 0.0f;
+            }
+            const float thxp[4] = {thc.y, thc.z, thc.w, thr}, thxm[4] = {thl, thc.x, thc.y, thc.z};
+            const float qxp[4] = {qvc.y, qvc.z, qvc.w, qr_}, qxm[4] = {ql, qvc.x, qvc.y, qvc.z};
+            float4 nvel, ch;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float Qenv = (qxp[k] + qxm[k] + comp(qf, k) + comp(qb, k)) / nv[k];
+                const float Tenv = (thxp[k] + thxm[k] + comp(thf, k) + comp(thb, k)) / nv[k];
+                const float psC = comp(pc, k);
+                const float psU = up ? comp(pu, k) : psC, psD = down ? comp(pd, k) : psC;
+                const float thU = up ? comp(thu, k) : 0.0f, thD = down ? comp(thd, k) : 0.0f;
+                const float QU = up ? comp(qvu, k) : 0.0f, QD = down ? comp(qvd, k) : 0.0f;
+                const float change = buoy_change(comp(vel, k), up, down, comp(pg, k), psC, psU, psD, comp(qvc, k), Qenv, QU, QD,
+                                                 comp(thc, k), thU, thD, comp(Tc, k), comp(Tu, k), comp(Td, k), comp(Wu, k),
+                                                 comp(Wd, k), Tenv, comp(tq, k), dt);
+                setc(ch, k, change);
+                setc(nvel, k, comp(vel, k) + change);
+            }
+            *reinterpret_cast<float4*>(v + c) = nvel;
+            if (dbg) *reinterpret_cast<float4*>(dbg + c) = ch;
+        }
+        thd = thc; qvd = qvc; pd = pc; Td = Tc; Wd = Wc;
+        thc = thu; qvc = qvu; pc = pu; Tc = Tu; Wc = Wu;
+    }
+}
+
 // initDensity Game/kernelSky.cu:1432-1452
 __global__ void __launch_bounds__(256) k_init_density(Grid g, float* __restrict__ rho, const float* __restrict__ th, const float* __restrict__ p,
                                                       const float* __restrict__ qv, const float* __restrict__ Pg) {
@@ -987,8 +1125,17 @@ void launch_precip3(Env& e, float dtS) {
 void launch_buoyancy(Env& e, float dtS) {
     ProfScope ps(e, "buoyancy");
     e.launches += 1;
-    k_buoyancy<<<cell_grid(e.g), dim3(BX, BY), 0, e.stream>>>(e.g, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.isenT, e.isenQv, e.p, e.Pg, dtS,
-                                                             (e.diag_flags & SKT_DIAG_BUOYANCY) ? e.dbg_buoy : nullptr);
+    float* dbg = (e.diag_flags & SKT_DIAG_BUOYANCY) ? e.dbg_buoy : nullptr;
+    const Grid& g = e.g;
+    if (e.flat && (g.X % 4) == 0) {
+        const int gx = (g.X / 4 + 31) / 32, gz = (g.Z + BZ4 - 1) / BZ4;
+        int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * 8 + gx * gz - 1) / (gx * gz)));
+        const int ylen = (g.Y - 1 + yc - 1) / yc;
+        yc = (g.Y - 1 + ylen - 1) / ylen;
+        k_buoyancy4<<<dim3(gx, gz, yc), dim3(32, BZ4), 0, e.stream>>>(g, ylen, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.p, e.Pg, dtS, dbg);
+        return;
+    }
+    k_buoyancy<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.isenT, e.isenQv, e.p, e.Pg, dtS, dbg);
 }
 void launch_init_density(Env& e) {
     ProfScope ps(e, "eos");

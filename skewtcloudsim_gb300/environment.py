@@ -310,3 +310,19 @@ class Environment:
     def reset_parameter(self, param):
         """resetParameterGPU."""
         self._check(self._L.skt_reset_parameter(self._h, int(param)))
+
+
+def step_ensemble(envs, dt, speed=1.0, nsteps: int = 1, threads: int = 0):
+    """skt_step_ensemble: advance every Environment in ``envs`` by ``nsteps`` steps at once (a
+    host thread per member drives its own stream). ``dt`` and ``speed`` are scalars or one value
+    per member. Returns the members' statuses; raises on the first failing member."""
+    L = _lib.load()
+    n = len(envs)
+    hs = (ctypes.c_void_p * n)(*[e._h.value if hasattr(e._h, "value") else e._h for e in envs])
+    dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float32), (n,)))
+    sps = np.ascontiguousarray(np.broadcast_to(np.asarray(speed, np.float32), (n,)))
+    st = (ctypes.c_int * n)()
+    rc = L.skt_step_ensemble(hs, n, _fp(dts), 0.0, _fp(sps), int(nsteps), int(threads), st)
+    if rc != 0:
+        raise SktError(rc, L.skt_last_error(None).decode())
+    return [Status(v) for v in st]

@@ -213,3 +213,35 @@ def workload(name: str, seed: Optional[int] = None, scale: Optional[tuple] = Non
         noise = 0.01
     st = make_initial_state(X, Y, Z, vox, snd, bubbles, wind_noise=noise, seed=seed + 1)
     return st, dt, 1.0
+
+
+# --------------------------------------------------------------------------------------------
+# The batched ensemble: members of uneven sizes, each with its own sounding and bubble.
+# --------------------------------------------------------------------------------------------
+
+ENSEMBLE_SIZES = ((64, 64, 32), (96, 96, 64), (128, 128, 64), (192, 192, 96))  # (x, y, z), z vertical
+
+
+def ensemble_members(n: int = 48, seed: int = 4000, sizes=ENSEMBLE_SIZES, scale: Optional[float] = None) -> list:
+    """``n`` members ``(InitialState, dt, speed)``: a size drawn uniformly from ``sizes``, surface
+    temperature U[290, 305] K, lapse rate U[5.5, 8] K/km to an 11 km tropopause, RH U[60, 95] %
+    below 1.5 km falling to 30 % at 6 km, one bubble of +1.5..3 K (R 500 m, 500 m up) at a random
+    horizontal position; 100 m cells, dt 0.5 s. Member m is seeded with ``seed + m``. ``scale``
+    shrinks every size by that factor (tests), keeping at least 8 cells and multiples of 4 in x."""
+    out = []
+    for m in range(n):
+        rng = np.random.default_rng(seed + m)
+        gx, gy, gz = sizes[int(rng.integers(len(sizes)))]
+        if scale is not None:
+            gx = max(8, int(round(gx * scale / 4)) * 4)
+            gy = max(8, int(round(gy * scale)))
+            gz = max(8, int(round(gz * scale)))
+        X, Y, Z = gx, gz, gy
+        vox = 100.0
+        snd = Sounding(Ts=float(rng.uniform(290.0, 305.0)), lapse=float(rng.uniform(5.5e-3, 8e-3)), tropopause=11000.0,
+                       ps=1000.0, rh=rh_piecewise(float(rng.uniform(0.60, 0.95)), 1500.0))
+        bubble = Bubble(float(rng.uniform(0.2, 0.8)) * X * vox, 500.0, float(rng.uniform(0.2, 0.8)) * Z * vox, 500.0,
+                        float(rng.uniform(1.5, 3.0)))
+        st = make_initial_state(X, Y, Z, vox, snd, [bubble], wind_noise=0.01, seed=seed + m + 100000)
+        out.append((st, 0.5, 1.0))
+    return out
