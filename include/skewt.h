@@ -79,7 +79,7 @@ typedef struct {
     float refine_tol;   /* MIXED: relative residual target of the FP64 refinement (1e-8) */
     int inner_max_iter; /* MIXED: FP32 iterations per refinement step */
     float inner_rtol;   /* MIXED: relative tolerance of each FP32 inner solve */
-    int use_graph;      /* capture the step in a CUDA graph (substep slots = max_substeps) */
+    int use_graph;      /* reserved, must be 0: the step is issued stream-ordered (no captured graph) */
     int mg_half;        /* MIXED: the V-cycle smooths with FP16 copies of the finest coefficients */
 } skt_solver_cfg;
 

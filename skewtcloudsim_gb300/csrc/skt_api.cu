@@ -243,6 +243,7 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     if (c.diffuse_sweeps < 0 || c.pcg_max_iter < 0 || c.max_substeps < 1 || (c.semantics != 0 && c.semantics != 1) ||
         (c.precision != 0 && c.precision != 1))
         return fail(nullptr, SKT_INVALID_ARG, "invalid solver configuration");
+    if (c.use_graph != 0) return fail(nullptr, SKT_INVALID_ARG, "use_graph is reserved: the step is not captured as a CUDA graph");
     skt_env* h = new (std::nothrow) skt_env();
     if (!h) return fail(nullptr, SKT_OUT_OF_MEMORY, "host allocation failed");
     Env& e = h->e;

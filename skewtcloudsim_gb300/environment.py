@@ -114,7 +114,7 @@ class SolverConfig:
     refine_tol: float = 1e-8
     inner_max_iter: int = 60
     inner_rtol: float = 1e-4
-    use_graph: int = 0
+    use_graph: int = 0          # reserved: must be 0 (no captured graph)
     mg_half: int = 1            # mixed: FP16 finest-level coefficients inside the V-cycle
 
     def c(self):

@@ -227,15 +227,14 @@ def ensemble_members(n: int = 48, seed: int = 4000, sizes=ENSEMBLE_SIZES, scale:
     temperature U[290, 305] K, lapse rate U[5.5, 8] K/km to an 11 km tropopause, RH U[60, 95] %
     below 1.5 km falling to 30 % at 6 km, one bubble of +1.5..3 K (R 500 m, 500 m up) at a random
     horizontal position; 100 m cells, dt 0.5 s. Member m is seeded with ``seed + m``. ``scale``
-    shrinks every size by that factor (tests), keeping at least 8 cells and multiples of 4 in x."""
+    shrinks every size by that factor (tests), to multiples of 8 cells (at least 8), which the
+    mixed solver's multigrid hierarchy can halve."""
     out = []
     for m in range(n):
         rng = np.random.default_rng(seed + m)
         gx, gy, gz = sizes[int(rng.integers(len(sizes)))]
         if scale is not None:
-            gx = max(8, int(round(gx * scale / 4)) * 4)
-            gy = max(8, int(round(gy * scale)))
-            gz = max(8, int(round(gz * scale)))
+            gx, gy, gz = (max(8, int(round(v * scale / 8)) * 8) for v in (gx, gy, gz))
         X, Y, Z = gx, gz, gy
         vox = 100.0
         snd = Sounding(Ts=float(rng.uniform(290.0, 305.0)), lapse=float(rng.uniform(5.5e-3, 8e-3)), tropopause=11000.0,
