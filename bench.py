@@ -15,7 +15,7 @@ resident in HBM (CUDA events on the library stream); "mixed" = the same step wit
 mixed-precision projection (FP32 multigrid-preconditioned CG inside float-float iterative
 refinement to a relative residual of 1e-8) and its speed-up over plain; e2e = the headline
 metric through the C ABI from host buffers (init H2D + per-step readback of every prognostic
-field, as the reference's per-step GPUSetEnv does); roofline = the dominant kernel's algorithmic
+field, as the reference's per-step GPUSetEnv does, overlapped with the next step); roofline = the dominant kernel's algorithmic
 bytes / its event-timed launch duration against the measured HBM copy bandwidth; step_roofline =
 algorithmic bytes of the whole step x cell-steps/s against the same peak; cpu_baseline = the
 oracle (CPU restatement) on the host cores on a bounded sub-box sample (all threads, and one
@@ -45,9 +45,9 @@ METRIC = "cell-steps/s at 512x512x256, mixed vs plain PCG at 1e-5 rel err; % HBM
 # Algorithmic bytes per cell per launch of each profiled stage (FP32 fields; each array counted
 # once per launch; neighbour re-reads excluded).
 STAGE_BYTES = {
-    "pcg_matvec": 24.0,   # s, ax, ay, az, aw read; As write
-    "pcg_update": 28.0,   # p, r read+write; s, As, aw read
-    "pcg_search": 16.0,   # r, aw read; s read+write
+    "pcg_matvec": 40.0,   # fused: z, s_old, aw, ax, ay, az read; p read+write; s_new, As write
+    "pcg_update": 20.0,   # fused: r read+write; As, aw read; z write
+    "pcg_search": 16.0,   # unfused (--pcg-fused 0): r, aw read; s read+write
     "diffuse": 8.0,       # per sweep: in read, out write
     "advect": 12.0,       # per pass: q, vel read; out write
     "micro": 64.0,        # 6 Q + th read/write, rho, p read (fused addHeat)
@@ -202,19 +202,20 @@ def run_reference(args, rank, world):
 def step_bytes(mode, pcg_iters, outer):
     """Algorithmic bytes per cell-step of the whole step (FP32, one advection substep): the stage
     total of the hot-path scope (2534 B; the three falling species share one march, 36 B instead
-    of 3 x 20) plus the pressure solve. Plain Jacobi-PCG: 52 B per
-    iteration. Mixed: per inner iteration the operator + search (32 B), the update (24 B) and the
+    of 3 x 20) plus the pressure solve. Plain Jacobi-PCG: 60 B per iteration (the operator with
+    the search step and the pressure update 40 B, the residual update with z = r/diag 20 B). Mixed: per inner iteration the operator + search (32 B), the update (24 B) and the
     V-cycle (93 B: four finest-level passes of 16-24.5 B with FP16 coefficients plus the coarser
     levels), per refinement step the float-float residual (32 B) and the correction (20 B)."""
     if mode == "plain":
-        return 2534.0 + 52.0 * pcg_iters
+        return 2534.0 + 60.0 * pcg_iters
     return 2534.0 + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
 
 
 def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
     from skewtcloudsim_gb300 import Environment, SolverConfig
     sem = args.semantics if mode == "plain" else 1
-    cfg = SolverConfig(semantics=sem, precision=1 if mode == "mixed" else 0, mg_half=args.mg_half)
+    cfg = SolverConfig(semantics=sem, precision=1 if mode == "mixed" else 0, mg_half=args.mg_half,
+                       pcg_fused=args.pcg_fused)
     env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
     env.init_from(init)
     for _ in range(args.warmup):
@@ -320,6 +321,8 @@ def main():
                     help="both: plain (reference semantics, the headline) and mixed (reported beside it)")
     ap.add_argument("--semantics", type=int, default=0)
     ap.add_argument("--mg-half", type=int, default=1, help="mixed: FP16 finest-level coefficients in the V-cycle")
+    ap.add_argument("--pcg-fused", type=int, default=1,
+                    help="plain: 1 = two launches per PCG iteration (search step fused into the operator), 0 = three")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--shape", default=None, help="x,y,z (z vertical) override of the workload size")
@@ -368,34 +371,33 @@ def main():
     # ---- end to end through the C ABI from host buffers (headline mode) -------------------
     e2e = None
     if not args.no_e2e and rank == 0:
-        import ctypes
-        import skewtcloudsim_gb300 as pkg
         names = ("th", "qv", "qw", "qc", "qr", "qs", "qi", "u", "v", "w", "p")
         host_in = {k: pinned_like(getattr(init, k)) for k in ("theta", "vel", "qv", "ground_T", "ground_p", "p3d",
                                                                "p_column")}
         outs = {k: pinned_like(np.empty(cells, np.float32)) for k in names}
         sem = args.semantics if head["mode"] == "plain" else 1
-        cfg = SolverConfig(semantics=sem, precision=1 if head["mode"] == "mixed" else 0, mg_half=args.mg_half)
+        cfg = SolverConfig(semantics=sem, precision=1 if head["mode"] == "mixed" else 0, mg_half=args.mg_half,
+                       pcg_fused=args.pcg_fused)
         env2 = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
         K = args.steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         env2.init(host_in["theta"][0], host_in["vel"][0], host_in["qv"][0], host_in["ground_T"][0],
                   host_in["ground_p"][0], host_in["p3d"][0], host_in["p_column"][0], init.ground_height)
+        host_outs = {k: outs[k][0] for k in names}
         for _ in range(K):
             env2.update_gpu(dt, speed)
-            for k in names:
-                a = outs[k][0]
-                prm, dr = pkg.FIELDS[k]
-                env2._check(env2._L.skt_read_field(env2._h, int(prm), int(dr), a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
-                                                   a.size))
+            env2.read_async(host_outs)  # this step's fields copy out while the next step runs
+        env2.read_wait()
         el = time.perf_counter() - t0
         h2d = sum(a[0].nbytes for a in host_in.values()) + init.ground_height.nbytes
         d2h = len(names) * cells * 4
         e2e = {"value": cells * K / el, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d / K),
                "d2h_bytes_per_step": int(d2h), "steps": K,
-               "note": "init from pinned host arrays once, then each step followed by the readback of the 11 "
-                       "prognostic fields (the reference's per-step GPUSetEnv); host wall clock"}
+               "note": "init from pinned host arrays once, then after each step the readback of the 11 "
+                       "prognostic fields into pinned host arrays (the reference's per-step GPUSetEnv), "
+                       "snapshot on the device and copied out on a second stream during the next step; "
+                       "host wall clock up to the last step's copies"}
         env2.close()
 
     cpu = None

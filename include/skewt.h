@@ -81,6 +81,9 @@ typedef struct {
     float inner_rtol;   /* MIXED: relative tolerance of each FP32 inner solve */
     int use_graph;      /* reserved, must be 0: the step is issued stream-ordered (no captured graph) */
     int mg_half;        /* MIXED: the V-cycle smooths with FP16 copies of the finest coefficients */
+    int pcg_fused;      /* PLAIN, nx % 4 == 0: two launches per iteration (search step and pressure
+                           update fused into the operator's march) instead of three; same values up
+                           to the dot products' summation order */
 } skt_solver_cfg;
 
 typedef struct {
@@ -137,6 +140,18 @@ skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float
 /* Field readback: the per-field copies of editor::GPUSetEnv (Game/editor.cpp:226-260).
  * dir selects the wind component for SKT_WIND. n must equal nx*ny*nz. Synchronous. */
 skt_status skt_read_field(skt_env* env, int param, int dir, float* host_dst, size_t n);
+
+/* Asynchronous readback of several fields (same selectors): the fields as they stand after the
+ * work queued so far are snapshot on the device, then copied to host_dsts[i] on a second stream,
+ * so that the next steps can run while the copies proceed; the call returns at once. A new
+ * snapshot first waits for the previous one's copies. The host buffers (n floats each, n =
+ * nx*ny*nz) must stay valid until skt_read_wait; pinned buffers let the copies overlap compute.
+ * The snapshot memory (nfields fields) is allocated by the first call that needs it. */
+skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, const int* dirs, float* const* host_dsts,
+                                 size_t n);
+
+/* Waits for the copies of the last skt_read_fields_async. */
+skt_status skt_read_wait(skt_env* env);
 
 /* Field upload (state injection); same selectors. Synchronous. */
 skt_status skt_write_field(skt_env* env, int param, int dir, const float* host_src, size_t n);

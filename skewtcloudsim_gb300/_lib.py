@@ -21,7 +21,7 @@ class SolverCfg(ctypes.Structure):
     _fields_ = [("semantics", ctypes.c_int), ("diffuse_sweeps", ctypes.c_int), ("pcg_tol", ctypes.c_float),
                 ("pcg_max_iter", ctypes.c_int), ("max_substeps", ctypes.c_int), ("precision", ctypes.c_int),
                 ("refine_tol", ctypes.c_float), ("inner_max_iter", ctypes.c_int), ("inner_rtol", ctypes.c_float),
-                ("use_graph", ctypes.c_int), ("mg_half", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("mg_half", ctypes.c_int), ("pcg_fused", ctypes.c_int)]
 
 
 class Sounding(ctypes.Structure):
@@ -51,6 +51,9 @@ SIGNATURES = {
     "skt_step_ensemble": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, c_float_p, ctypes.c_float, c_float_p,
                                          ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "skt_read_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_float_p, ctypes.c_size_t]),
+    "skt_read_fields_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(c_float_p), ctypes.c_size_t]),
+    "skt_read_wait": (ctypes.c_int, [ctypes.c_void_p]),
     "skt_write_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_float_p, ctypes.c_size_t]),
     "skt_field_device_ptr": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(c_float_p)]),
     "skt_read_ground": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p, ctypes.c_size_t]),

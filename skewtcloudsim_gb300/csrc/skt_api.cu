@@ -153,6 +153,21 @@ skt_status report(Env* e, skt_status st, const char* msg) { return fail(e, st, m
 float* field_ptr(Env& e, int param, int dir) { return sky_ptr(e, param, dir); }
 float* ground_field_ptr(Env& e, int which) { return ground_ptr(e, which); }
 skt_status check_cuda(Env& e, const char* where) { return cuda_check(e, where); }
+__global__ void k_fetch_sc(const unsigned* __restrict__ src, unsigned* dst, int nwords) {
+    for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+}
+__global__ void k_snapshot(const float4* __restrict__ src, float4* __restrict__ dst, size_t n4) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n4; i += size_t(gridDim.x) * blockDim.x) dst[i] = src[i];
+}
+
+void fetch_scalars(Env& e) {
+    static_assert(sizeof(Scalars) % 4 == 0, "Scalars is copied as 32-bit words");
+    k_fetch_sc<<<1, 32, 0, e.stream>>>(reinterpret_cast<const unsigned*>(e.sc), reinterpret_cast<unsigned*>(e.host_sc_dev),
+                                       int(sizeof(Scalars) / 4));
+    e.launches += 1;
+    cudaStreamSynchronize(e.stream);
+}
+
 }  // namespace skt
 
 extern "C" {
@@ -170,6 +185,7 @@ void skt_default_config(skt_solver_cfg* c) {
     c->inner_rtol = 1e-4f;
     c->use_graph = 0;
     c->mg_half = 1;
+    c->pcg_fused = 1;
 }
 
 skt_status skt_set_rate_region(skt_env* env, int enable, const int lo[3], const int hi[3]) {
@@ -256,7 +272,7 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     e.g.N = int(n);
     e.g.vox = grid->voxel;
     e.cfg = SolverCfg{c.semantics, c.diffuse_sweeps, c.pcg_tol, c.pcg_max_iter, c.max_substeps, c.precision, c.refine_tol, c.inner_max_iter,
-                      c.inner_rtol, c.use_graph, c.mg_half};
+                      c.inner_rtol, c.use_graph, c.mg_half, c.pcg_fused};
     const size_t N = size_t(n), NG = size_t(grid->nx) * grid->nz, NY = size_t(grid->ny);
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const int nsky = 12 + 2 + 4 + 4;
@@ -290,8 +306,10 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     e.partials = (double*)take(sizeof(double) * 2 * kMaxPartials);
     cudaMemsetAsync(e.pool, 0, bytes, e.stream);
     e.g.gh = e.gh;
-    if (cudaMallocHost(&e.host_sc, sizeof(Scalars)) != cudaSuccess) {
+    if (cudaMallocHost(&e.host_sc, sizeof(Scalars)) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&e.host_sc_dev, e.host_sc, 0) != cudaSuccess) {
         cudaGetLastError();
+        if (e.host_sc) cudaFreeHost(e.host_sc);
         cudaFree(e.pool);
         cudaStreamDestroy(e.stream);
         delete h;
@@ -345,6 +363,11 @@ void skt_destroy(skt_env* env) {
     if (e.rates_dev) cudaFree(e.rates_dev);
     if (e.dbg_buoy) cudaFree(e.dbg_buoy);
     if (e.dbg_zero) cudaFree(e.dbg_zero);
+    if (e.copy_stream) cudaStreamSynchronize(e.copy_stream);
+    if (e.snap) cudaFree(e.snap);
+    if (e.ev_snap) cudaEventDestroy(e.ev_snap);
+    if (e.ev_copy) cudaEventDestroy(e.ev_copy);
+    if (e.copy_stream) cudaStreamDestroy(e.copy_stream);
     if (e.brick_flags) cudaFree(e.brick_flags);
     if (e.brick_out) cudaFree(e.brick_out);
     if (e.host_sc) cudaFreeHost(e.host_sc);
@@ -410,8 +433,8 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
     const skt_status st = cuda_check(e, "step");
     if (st != SKT_OK) return st;
-    int dev_status = 0;
-    cudaMemcpy(&dev_status, &e.sc->status, sizeof(int), cudaMemcpyDeviceToHost);
+    fetch_scalars(e);
+    const int dev_status = e.host_sc->status;
     if (dev_status != 0) {
         cudaMemset(&e.sc->status, 0, sizeof(int));
         return fail(&e, skt_status(dev_status), "a kernel gave up waiting for its streamed data (device-side wait limit)");
@@ -469,6 +492,65 @@ skt_status skt_read_field(skt_env* env, int param, int dir, float* dst, size_t n
     cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToHost, e.stream);
     cudaStreamSynchronize(e.stream);
     return cuda_check(e, "read_field");
+}
+
+skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, const int* dirs, float* const* dst, size_t n) {
+    if (!env || nfields < 0 || (nfields > 0 && (!params || !dst))) return fail(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    if (n != size_t(e.g.N)) return fail(&e, SKT_INVALID_ARG, "size mismatch");
+    std::vector<float*> src(nfields);
+    for (int i = 0; i < nfields; ++i) {
+        src[i] = sky_ptr(e, params[i], dirs ? dirs[i] : 0);
+        if (!src[i] || !dst[i]) return fail(&e, SKT_INVALID_ARG, "unknown field selector or null destination");
+    }
+    if (!e.copy_stream) {
+        if (cudaStreamCreateWithFlags(&e.copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&e.ev_snap, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&e.ev_copy, cudaEventDisableTiming) != cudaSuccess)
+            return cuda_check(e, "read_fields_async");
+    }
+    if (e.snap_fields < size_t(nfields)) {
+        if (e.copy_pending) cudaEventSynchronize(e.ev_copy);
+        if (e.snap) cudaFree(e.snap);
+        e.snap = nullptr;
+        e.snap_fields = 0;
+        if (cudaMalloc(&e.snap, sizeof(float) * n * size_t(nfields)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(&e, SKT_OUT_OF_MEMORY, "snapshot allocation failed");
+        }
+        e.snap_fields = size_t(nfields);
+        e.copy_pending = false;
+    }
+    // the snapshot waits for the copies of the previous one, then follows the queued work
+    if (e.copy_pending) cudaStreamWaitEvent(e.stream, e.ev_copy, 0);
+    // the snapshot is an SM copy (a kernel on the step's stream), so it never waits for a copy engine
+    for (int i = 0; i < nfields; ++i) {
+        float* d = e.snap + size_t(i) * n;
+        if (n % 4 == 0) {
+            const size_t n4 = n / 4;
+            const int blocks = int(std::min<size_t>((n4 + 255) / 256, size_t(e.num_sms) * 8));
+            k_snapshot<<<blocks, 256, 0, e.stream>>>(reinterpret_cast<const float4*>(src[i]), reinterpret_cast<float4*>(d), n4);
+        } else {
+            cudaMemcpyAsync(d, src[i], sizeof(float) * n, cudaMemcpyDeviceToDevice, e.stream);
+        }
+    }
+    cudaEventRecord(e.ev_snap, e.stream);
+    cudaStreamWaitEvent(e.copy_stream, e.ev_snap, 0);
+    for (int i = 0; i < nfields; ++i)
+        cudaMemcpyAsync(dst[i], e.snap + size_t(i) * n, sizeof(float) * n, cudaMemcpyDeviceToHost, e.copy_stream);
+    cudaEventRecord(e.ev_copy, e.copy_stream);
+    e.copy_pending = true;
+    return cuda_check(e, "read_fields_async");
+}
+
+skt_status skt_read_wait(skt_env* env) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (e.copy_pending) {
+        cudaEventSynchronize(e.ev_copy);
+        e.copy_pending = false;
+    }
+    return cuda_check(e, "read_wait");
 }
 
 skt_status skt_write_field(skt_env* env, int param, int dir, const float* src, size_t n) {

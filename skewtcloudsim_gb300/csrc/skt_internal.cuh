@@ -68,6 +68,7 @@ __device__ __forceinline__ float face_nb(const Grid& g, const float* __restrict_
 struct Scalars {
     double sigma0, sigma1, beta;      // PCG scalars (FP64)
     float alpha, beta_f;              // the FP32 step lengths applied to the vectors
+    float alpha_pp;                   // plain PCG: the step length of the pressure update still to apply
     unsigned int maxbits;             // float bits of a max-reduction (atomicMax on uint)
     int converged;                    // PCG stop flag
     int iters;                        // PCG iterations done
@@ -107,6 +108,7 @@ struct SolverCfg {
     float inner_rtol;
     int use_graph;
     int mg_half;         // mixed: FP16 finest-level coefficients in the V-cycle
+    int pcg_fused;       // plain: search step and pressure update fused into the operator
 };
 
 struct Env {
@@ -134,8 +136,8 @@ struct Env {
     // reductions
     Scalars* sc;
     double* partials;
-    float* host_scalars;  // pinned
-    Scalars* host_sc;     // pinned mirror
+    Scalars* host_sc = nullptr;      // pinned mirror, written by fetch_scalars
+    Scalars* host_sc_dev = nullptr;  // the mirror's device-side address (mapped pinned memory)
     // host clock (environmentGPU::m_time etc.)
     float sim_time = 43200.0f;
     int day = 130;
@@ -169,6 +171,12 @@ struct Env {
     int* brick_flags = nullptr;   // per 8^3 brick: active, then its output slot
     int* brick_count = nullptr;
     void* brick_out = nullptr;    // packed brick values and coordinates
+    // asynchronous readback: a device snapshot of the fields and the stream that copies it out
+    float* snap = nullptr;
+    size_t snap_fields = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_snap = nullptr, ev_copy = nullptr;
+    bool copy_pending = false;
     size_t brick_out_bytes = 0;
     int diag_flags = 0;
     float* dbg_buoy = nullptr;    // buoyancy velocity change per cell (the second debug field)
@@ -225,6 +233,10 @@ void mg_solve(Env& e);
 skt_status report(Env* e, skt_status st, const char* msg);
 skt_status check_cuda(Env& e, const char* where);
 // the device array behind a field selector (skt_read_field's mapping), nullptr if none
+// Copies the device scalars into the pinned mirror e.host_sc with a one-warp kernel (stores to
+// mapped host memory) and waits for the stream: the step's control reads never queue behind
+// bulk copies on the copy engines.
+void fetch_scalars(Env& e);
 float* field_ptr(Env& e, int param, int dir);
 float* ground_field_ptr(Env& e, int which);
 

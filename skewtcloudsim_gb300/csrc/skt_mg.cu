@@ -1195,8 +1195,7 @@ void mg_solve(Env& e) {
             }
             e.launches += 1;
         }
-        cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-        cudaStreamSynchronize(e.stream);
+        fetch_scalars(e);
         if (e.host_sc->refine_done == 1) break;
         // inner MG-PCG on A e = r
         const int* conv = &e.sc->converged;
@@ -1221,8 +1220,7 @@ void mg_solve(Env& e) {
                     { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NEXT); }
                     std::swap(s_old, s_new);
                 }
-                cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-                cudaStreamSynchronize(e.stream);
+                fetch_scalars(e);
                 if (e.host_sc->converged) break;
             }
             { ProfScope ps(e, "mg_refine");
@@ -1264,8 +1262,7 @@ void mg_solve(Env& e) {
                   k_search_mg<<<nb, RT, 0, e.stream>>>(n, z0, e.s, e.sc); }
                 e.launches += 4;
             }
-            cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-            cudaStreamSynchronize(e.stream);
+            fetch_scalars(e);
             if (e.host_sc->converged) break;
         }
         { ProfScope ps(e, "mg_refine");
@@ -1274,8 +1271,7 @@ void mg_solve(Env& e) {
     }
     k_cast_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, e.pp);
     e.launches += 1;
-    cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-    cudaStreamSynchronize(e.stream);
+    fetch_scalars(e);
     e.last_outer = outer;
     e.last_iters = e.host_sc->outer_inner_total;
     e.last_residual = float(e.host_sc->rnorm0 > 0 ? e.host_sc->rnorm / e.host_sc->rnorm0 : 0.0);

@@ -510,6 +510,183 @@ __global__ void __launch_bounds__(MVT) k_matvec4(Grid g, int zlen, const float* 
     }
 }
 
+// ---- fused PCG iteration (X % 4 == 0): two launches per iteration instead of three --------
+// The search step (endIteration :987-1014) and the next matrix product share one z march, and
+// the pressure update of the previous iteration (updatePandDiv :955-985, p += alpha s) rides
+// along where s_old is read anyway. The residual kernel stores z = r/diag (it forms z for z.r in
+// any case), so the operator forms s_new = z + beta s_old from two arrays wherever it needs a
+// neighbour's value. Every value is formed as in k_search4 / k_update4 (the search direction as
+// fma(beta, s_old, z), the pressure as fma(alpha, s, p)); only the dot products' summation order
+// differs.
+
+// s_new = z + beta s_old, As = A s_new, s_new.As -> alpha, and p += alpha_pp s_old. The rows
+// above and below and the next plane form their s_new from z and s_old (another warp's or
+// block's rows, read through L1/L2); the x neighbours come from the neighbouring lanes. s_old
+// and s_new are distinct buffers (a block's halo rows are another block's own rows, so s cannot
+// be updated in place).
+template <bool FLAT>
+__global__ void __launch_bounds__(MVT) k_matvec_search4(Grid g, int zlen, const float* __restrict__ ax, const float* __restrict__ ay,
+                                                        const float* __restrict__ az, const float* __restrict__ aw,
+                                                        const float* __restrict__ zv, const float* __restrict__ sold,
+                                                        float* __restrict__ snew, float* __restrict__ As, float* __restrict__ pp,
+                                                        int reference, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ double smd[MVT / 32];
+    const float beta = sc->beta_f, alpha_pp = sc->alpha_pp;
+    const int lane = threadIdx.x, tid = threadIdx.x + 32 * threadIdx.y;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * MVY + threadIdx.y;
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const int X = g.X, XY = g.XY;
+    const int row = x0 + y * X;
+    auto srow = [&](int c) {
+        const float4 z = ld4(zv, c), so = ld4(sold, c);
+        return make_float4(__fmaf_rn(beta, so.x, z.x), __fmaf_rn(beta, so.y, z.y), __fmaf_rn(beta, so.z, z.z), __fmaf_rn(beta, so.w, z.w));
+    };
+    auto sone = [&](int c) { return __fmaf_rn(beta, sold[c], zv[c]); };
+    Kahan acc;
+    float4 vb = f4zero(), vc = f4zero(), azb = f4zero();
+    if (act) {
+        const int c = row + zs * XY;
+        vc = srow(c);
+        if (zs > 0) { vb = srow(c - XY); azb = ld4(az, c - XY); }
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 vf = f4zero(), vd = f4zero(), vu = f4zero(), ayd = f4zero(), cx = f4zero(), cy = f4zero(), cz = f4zero(), cw = f4zero();
+        int4 gh4 = make_int4(0, 0, 0, 0);
+        if (act) {
+            if (z + 1 < g.Z) vf = srow(c + XY);
+            if (y > 0) { vd = srow(c - X); ayd = ld4(ay, c - X); }
+            if (y + 1 < g.Y) vu = srow(c + X);
+            cx = ld4(ax, c); cy = ld4(ay, c); cz = ld4(az, c); cw = ld4(aw, c);
+            if (!FLAT) gh4 = *reinterpret_cast<const int4*>(g.gh + x0 + z * X);
+            // the previous iteration's pressure update (s_old of this row was read for vc)
+            const float4 so = ld4(sold, c);
+            float4 pv = ld4(pp, c);
+            pv.x = __fmaf_rn(alpha_pp, so.x, pv.x);
+            pv.y = __fmaf_rn(alpha_pp, so.y, pv.y);
+            pv.z = __fmaf_rn(alpha_pp, so.z, pv.z);
+            pv.w = __fmaf_rn(alpha_pp, so.w, pv.w);
+            *reinterpret_cast<float4*>(pp + c) = pv;
+        }
+        float sl = __shfl_up_sync(0xffffffffu, vc.w, 1);
+        float axl = __shfl_up_sync(0xffffffffu, cx.w, 1);
+        float sr = __shfl_down_sync(0xffffffffu, vc.x, 1);
+        if (act && lane == 0) {
+            if (x0 > 0) { sl = sone(c - 1); axl = ax[c - 1]; } else { sl = 0.0f; axl = 0.0f; }
+        }
+        if (act && (lane == 31 || x0 + 4 >= X)) sr = (x0 + 4 < X) ? sone(c + 4) : 0.0f;
+        if (act) {
+            float AL0 = axl, AL1 = cx.x, AL2 = cx.y, AL3 = cx.z;
+            float AD0 = ayd.x, AD1 = ayd.y, AD2 = ayd.z, AD3 = ayd.w;
+            float AB0 = azb.x, AB1 = azb.y, AB2 = azb.z, AB3 = azb.w;
+            if (reference) {
+                AL0 = char_trunc(AL0); AL1 = char_trunc(AL1); AL2 = char_trunc(AL2); AL3 = char_trunc(AL3);
+                AD0 = char_trunc(AD0); AD1 = char_trunc(AD1); AD2 = char_trunc(AD2); AD3 = char_trunc(AD3);
+                AB0 = char_trunc(AB0); AB1 = char_trunc(AB1); AB2 = char_trunc(AB2); AB3 = char_trunc(AB3);
+            }
+            float4 o;
+            o.x = cw.x * vc.x + ((AL0 * sl + AD0 * vd.x + AB0 * vb.x + cx.x * vc.y + cy.x * vu.x + cz.x * vf.x));
+            o.y = cw.y * vc.y + ((AL1 * vc.x + AD1 * vd.y + AB1 * vb.y + cx.y * vc.z + cy.y * vu.y + cz.y * vf.y));
+            o.z = cw.z * vc.z + ((AL2 * vc.y + AD2 * vd.z + AB2 * vb.z + cx.z * vc.w + cy.z * vu.z + cz.z * vf.z));
+            o.w = cw.w * vc.w + ((AL3 * vc.z + AD3 * vd.w + AB3 * vb.w + cx.w * sr + cy.w * vu.w + cz.w * vf.w));
+            if (FLAT) {
+                if (y == 0) o = f4zero();
+            } else {
+                if (y <= gh4.x) o.x = 0.0f;
+                if (y <= gh4.y) o.y = 0.0f;
+                if (y <= gh4.z) o.z = 0.0f;
+                if (y <= gh4.w) o.w = 0.0f;
+            }
+            *reinterpret_cast<float4*>(snew + c) = vc;
+            *reinterpret_cast<float4*>(As + c) = o;
+            acc.add(o.x * vc.x);
+            acc.add(o.y * vc.y);
+            acc.add(o.z * vc.z);
+            acc.add(o.w * vc.w);
+        }
+        vb = vc;
+        vc = vf;
+        azb = cz;
+    }
+    const double bs = block_sum_n<MVT>(double(acc.s) - double(acc.c), smd, tid);
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    double tot;
+    float mall;
+    if (publish_n<MVT>(sc, partials, bid, nb, tid, bs, 0.0f, tot, mall)) {
+        const double s1 = reference ? sc->sigma1 + tot : tot;
+        sc->sigma1 = s1;
+        sc->alpha = float(sc->sigma0 / s1);
+    }
+}
+
+// r -= alpha As, z = r/diag (stored), z.r and the max residual: k_update4 without the pressure
+// update, which the next k_matvec_search4 or k_pressure_tail4 applies with alpha_pp = alpha
+__global__ void __launch_bounds__(UT) k_residual4(int n4, int xy4, const float4* __restrict__ aw, const float4* __restrict__ As,
+                                                  float4* __restrict__ r, float4* __restrict__ zout, int reference, float tol,
+                                                  int max_iter, Scalars* sc, double* partials) {
+    if (sc->converged) return;
+    __shared__ double smd[UT / 32];
+    __shared__ float smf[UT / 32];
+    const float alpha = sc->alpha;
+    Kahan acc;
+    float mx = 0.0f;
+    for (int i = blockIdx.x * UT + threadIdx.x; i < n4; i += gridDim.x * UT) {
+        const float4 a = aw[i], av = As[i];
+        float4 rv = r[i];
+        rv.x = rv.x - alpha * av.x; rv.y = rv.y - alpha * av.y; rv.z = rv.z - alpha * av.z; rv.w = rv.w - alpha * av.w;
+        r[i] = rv;
+        const float z0 = rv.x * precon_of(a.x), z1 = rv.y * precon_of(a.y), z2 = rv.z * precon_of(a.z), z3 = rv.w * precon_of(a.w);
+        zout[i] = make_float4(z0, z1, z2, z3);
+        acc.add(z0 * rv.x);
+        acc.add(z1 * rv.y);
+        acc.add(z2 * rv.z);
+        acc.add(z3 * rv.w);
+        const bool absv = !reference || i < xy4;  // the reference takes |r| on the z = 0 plane only (Q4)
+        const float m0 = absv ? fabsf(rv.x) : rv.x, m1 = absv ? fabsf(rv.y) : rv.y;
+        const float m2 = absv ? fabsf(rv.z) : rv.z, m3 = absv ? fabsf(rv.w) : rv.w;
+        if (m0 > mx) mx = m0;
+        if (m1 > mx) mx = m1;
+        if (m2 > mx) mx = m2;
+        if (m3 > mx) mx = m3;
+    }
+    const double bs = block_sum_n<UT>(double(acc.s) - double(acc.c), smd, threadIdx.x);
+    const float bm = block_max_n<UT>(mx, smf, threadIdx.x);
+    double tot;
+    float mall;
+    if (publish_n<UT>(sc, partials, blockIdx.x, gridDim.x, threadIdx.x, bs, bm, tot, mall)) {
+        sc->iters += 1;
+        sc->residual = mall;
+        sc->alpha_pp = alpha;
+        if (mall <= tol) {
+            sc->converged = 1;
+        } else if (sc->iters >= max_iter) {
+            sc->converged = 2;
+        } else {
+            sc->sigma1 = tot;
+            sc->beta_f = float(tot / sc->sigma0);
+            sc->sigma0 = tot;
+        }
+    }
+}
+
+// the last iteration's pressure update: p += alpha_pp s
+__global__ void __launch_bounds__(UT) k_pressure_tail4(int n4, const float4* __restrict__ s, float4* __restrict__ pp, const Scalars* sc) {
+    const float alpha = sc->alpha_pp;
+    for (int i = blockIdx.x * UT + threadIdx.x; i < n4; i += gridDim.x * UT) {
+        const float4 sv = s[i];
+        float4 pv = pp[i];
+        pv.x = __fmaf_rn(alpha, sv.x, pv.x);
+        pv.y = __fmaf_rn(alpha, sv.y, pv.y);
+        pv.z = __fmaf_rn(alpha, sv.z, pv.z);
+        pv.w = __fmaf_rn(alpha, sv.w, pv.w);
+        pp[i] = pv;
+    }
+}
+
 // k_build for flat terrain and X % 4 == 0: four cells per thread, a march along z in blocks of
 // MVY rows. Each cell's reciprocal density is formed once (the x neighbours' by shuffle, the next
 // plane's carried), and each face once: a cell forms its right, up and front faces; the left face
@@ -761,10 +938,34 @@ void launch_project(Env& e, float dtS) {
     const int zlen = (g.Z + zc - 1) / zc;
     zc = (g.Z + zlen - 1) / zlen;
     const dim3 mvg(gx, gy, zc);
+    // fused iterations: the search directions alternate between e.s and e.tB, z = r/diag lives in
+    // e.tA (both free during the projection: the advection's scratch); iteration k's direction is
+    // dirs[k % 2]
+    float* dirs[2] = {e.s, e.tB};
+    float* zbuf = e.tA;
     for (int it = 0; it < e.cfg.pcg_max_iter; it += chunk) {
         const int n = std::min(chunk, e.cfg.pcg_max_iter - it);
         for (int k = 0; k < n; ++k) {
-            if (vec) {
+            if (vec && e.cfg.pcg_fused) {
+                const int kk = it + k;
+                float* sd = dirs[kk & 1];
+                { ProfScope ps(e, "pcg_matvec"); e.launches += 1;
+                  if (kk == 0) {  // the first direction is z itself (set by the build)
+                      if (e.flat) k_matvec4<true><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, sd, e.As, ref, e.sc, e.partials);
+                      else k_matvec4<false><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, sd, e.As, ref, e.sc, e.partials);
+                  } else {
+                      const float* so = dirs[(kk - 1) & 1];
+                      if (e.flat)
+                          k_matvec_search4<true><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, zbuf, so, sd, e.As, e.pp, ref,
+                                                                            e.sc, e.partials);
+                      else
+                          k_matvec_search4<false><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, zbuf, so, sd, e.As, e.pp, ref,
+                                                                             e.sc, e.partials);
+                  } }
+                { ProfScope ps(e, "pcg_update"); e.launches += 1;
+                  k_residual4<<<nstream, UT, 0, e.stream>>>(n4, g.XY / 4, (const float4*)e.aw, (const float4*)e.As, (float4*)e.r,
+                                                            (float4*)zbuf, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
+            } else if (vec) {
                 { ProfScope ps(e, "pcg_matvec"); e.launches += 1;
                   if (e.flat) k_matvec4<true><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials);
                   else k_matvec4<false><<<mvg, mvb, 0, e.stream>>>(g, zlen, e.ax, e.ay, e.az, e.aw, e.s, e.As, ref, e.sc, e.partials); }
@@ -779,9 +980,14 @@ void launch_project(Env& e, float dtS) {
                 { ProfScope ps(e, "pcg_search"); e.launches += 1; k_search<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.r, e.s, e.sc); }
             }
         }
-        cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-        cudaStreamSynchronize(e.stream);
+        fetch_scalars(e);
         if (e.host_sc->converged) break;
+    }
+    if (vec && e.cfg.pcg_fused && e.host_sc->iters > 0) {
+        // the last iteration's pressure update (no later operator launch carried it)
+        ProfScope ps(e, "pcg_update");
+        e.launches += 1;
+        k_pressure_tail4<<<nstream, UT, 0, e.stream>>>(n4, (const float4*)dirs[(e.host_sc->iters - 1) & 1], (float4*)e.pp, e.sc);
     }
     e.last_iters = e.host_sc->iters;
     e.last_residual = e.host_sc->residual;

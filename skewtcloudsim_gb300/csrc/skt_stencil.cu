@@ -987,8 +987,7 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
         k_nsub<<<1, 1, 0, e.stream>>>(e.sc, dtS, g.vox, float(e.cfg.max_substeps));
         e.adv_nsub = -1;
         if (host_sync) {
-            cudaMemcpyAsync(e.host_sc, e.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, e.stream);
-            cudaStreamSynchronize(e.stream);
+            fetch_scalars(e);
             e.adv_nsub = e.host_sc->nsub;
         } else {
             e.adv_nsub = 0;  // on the device only (sc->nsub)

@@ -116,11 +116,12 @@ class SolverConfig:
     inner_rtol: float = 1e-4
     use_graph: int = 0          # reserved: must be 0 (no captured graph)
     mg_half: int = 1            # mixed: FP16 finest-level coefficients inside the V-cycle
+    pcg_fused: int = 1          # plain: search step and pressure update fused into the operator
 
     def c(self):
         return _lib.SolverCfg(self.semantics, self.diffuse_sweeps, self.pcg_tol, self.pcg_max_iter, self.max_substeps,
                               self.precision, self.refine_tol, self.inner_max_iter, self.inner_rtol, self.use_graph,
-                              self.mg_half)
+                              self.mg_half, self.pcg_fused)
 
 
 def _fp(a):
@@ -211,6 +212,25 @@ class Environment:
         else:
             raise KeyError(name)
         return out
+
+    def read_async(self, outs: dict):
+        """skt_read_fields_async: queue the readback of the fields named in ``outs`` (name -> float32
+        array of n values, ideally pinned) as they stand after the queued work; returns at once.
+        The arrays must stay alive until ``read_wait``."""
+        names = list(outs)
+        prm = (ctypes.c_int * len(names))(*[int(FIELDS[k][0]) for k in names])
+        drs = (ctypes.c_int * len(names))(*[int(FIELDS[k][1]) for k in names])
+        for k in names:
+            a = outs[k]
+            if a.dtype != np.float32 or a.size != self.n or not a.flags.c_contiguous:
+                raise ValueError(f"{k}: need a contiguous float32 array of {self.n} values")
+        dst = (_lib.c_float_p * len(names))(*[_fp(outs[k]) for k in names])
+        self._pending_reads = outs  # keep the buffers alive until read_wait
+        self._check(self._L.skt_read_fields_async(self._h, len(names), prm, drs, dst, self.n))
+
+    def read_wait(self):
+        self._check(self._L.skt_read_wait(self._h))
+        self._pending_reads = None
 
     def write(self, name: str, a):
         a = np.ascontiguousarray(a, np.float32)

@@ -237,3 +237,38 @@ def test_full_step_parity_terrain(gpu_lib):
         assert not bad, (step, bad)
         push_oracle_to_env(st, env)
     env.close()
+
+
+
+@pytest.mark.parametrize("sem,terrain", [(0, False), (1, False), (0, True)])
+def test_projection_fused_iteration_matches_three_launch(gpu_lib, sem, terrain):
+    """The two-launch PCG iteration (search step and pressure update fused into the operator's
+    march, directions alternating between two buffers) against the three-launch one on the same
+    state: the same iteration count within one (only the dot products' summation order differs),
+    the same fields to the step tolerance (rounding differences of a hundred CG iterations), and
+    both within the stage tolerance of the oracle."""
+    init, dt, speed = small_case(SHAPE)
+    if terrain:
+        xx, zz = np.meshgrid(np.arange(init.nx), np.arange(init.nz))
+        init.ground_height = np.clip(np.round(3.0 * np.exp(-((xx - 12) ** 2 + (zz - 18) ** 2) / 40.0)), 0,
+                                     3).astype(np.int32).reshape(-1)
+    st0 = oracle.OracleState(init, np.float32)
+    for _ in range(2):
+        st0.step(oracle_cfg(), dt, speed)
+    st = _clone(st0)
+    o = st.stage(oracle_cfg(sem), 3, 0, dt * speed)
+    got = {}
+    for fused in (1, 0):
+        env = make_env(init, gpu_cfg(sem, pcg_fused=fused))
+        push_oracle_to_env(st0, env)
+        g = env.run_stage(3, 0, dt * speed)
+        got[fused] = (g["pcg_iters"], {k: env.read(k) for k in ("u", "v", "w", "p")})
+        assert abs(g["pcg_iters"] - o["pcg_iters"]) <= 1, (fused, g, o)
+        res = compare(env, st, names=("u", "v", "w", "p", "rho"), ground=())
+        for k, (l2, mx) in res.items():
+            assert l2 <= 1e-5, (fused, k, l2, mx)
+        env.close()
+    assert abs(got[1][0] - got[0][0]) <= 1
+    m = st.sky_mask()
+    for k in ("u", "v", "w", "p"):
+        assert rel_l2(got[1][1][k], got[0][1][k], m) <= STEP_TOL, k
