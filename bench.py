@@ -396,8 +396,8 @@ def main():
                "d2h_bytes_per_step": int(d2h), "steps": K,
                "note": "init from pinned host arrays once, then after each step the readback of the 11 "
                        "prognostic fields into pinned host arrays (the reference's per-step GPUSetEnv), "
-                       "snapshot on the device and copied out on a second stream during the next step; "
-                       "host wall clock up to the last step's copies"}
+                       "snapshot on the device and written into the pinned arrays by a kernel on a second "
+                       "stream during the next step; host wall clock up to the last step's copies"}
         env2.close()
 
     cpu = None

@@ -160,6 +160,8 @@ __global__ void k_snapshot(const float4* __restrict__ src, float4* __restrict__ 
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n4; i += size_t(gridDim.x) * blockDim.x) dst[i] = src[i];
 }
 
+constexpr int kHostCopyBlocks = 64;  // blocks of the kernel that writes a snapshot to mapped host memory
+
 void fetch_scalars(Env& e) {
     static_assert(sizeof(Scalars) % 4 == 0, "Scalars is copied as 32-bit words");
     k_fetch_sc<<<1, 32, 0, e.stream>>>(reinterpret_cast<const unsigned*>(e.sc), reinterpret_cast<unsigned*>(e.host_sc_dev),
@@ -536,8 +538,21 @@ skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, c
     }
     cudaEventRecord(e.ev_snap, e.stream);
     cudaStreamWaitEvent(e.copy_stream, e.ev_snap, 0);
-    for (int i = 0; i < nfields; ++i)
-        cudaMemcpyAsync(dst[i], e.snap + size_t(i) * n, sizeof(float) * n, cudaMemcpyDeviceToHost, e.copy_stream);
+    // pinned destinations are written by a narrow kernel through their mapped addresses (it takes a
+    // few SMs beside the next step's kernels); pageable ones by the copy engine
+    for (int i = 0; i < nfields; ++i) {
+        const float* s = e.snap + size_t(i) * n;
+        cudaPointerAttributes at{};
+        const bool mapped = cudaPointerGetAttributes(&at, dst[i]) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer &&
+                            (reinterpret_cast<uintptr_t>(at.devicePointer) % 16) == 0 && n % 4 == 0;
+        cudaGetLastError();
+        if (mapped) {
+            k_snapshot<<<kHostCopyBlocks, 256, 0, e.copy_stream>>>(reinterpret_cast<const float4*>(s), static_cast<float4*>(at.devicePointer), n / 4);
+            e.launches += 1;
+        } else {
+            cudaMemcpyAsync(dst[i], s, sizeof(float) * n, cudaMemcpyDeviceToHost, e.copy_stream);
+        }
+    }
     cudaEventRecord(e.ev_copy, e.copy_stream);
     e.copy_pending = true;
     return cuda_check(e, "read_fields_async");

@@ -1,6 +1,7 @@
 """Asynchronous readback (skt_read_fields_async / skt_read_wait): the fields arrive as they stood
 when the call was made, even though the next step is already running on the device, and match
-the synchronous skt_read_field bit for bit."""
+the synchronous skt_read_field bit for bit, into pageable (copy engine) and pinned (a kernel
+storing through the mapped address) host buffers."""
 import numpy as np
 import pytest
 
@@ -11,8 +12,22 @@ pytestmark = pytest.mark.gpu
 NAMES = ("th", "qv", "qw", "qc", "qr", "qs", "qi", "u", "v", "w", "p")
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_async_readback_is_the_snapshot(gpu_lib, precision):
+def _host_buffers(n, pinned, keep):
+    """Pinned buffers take the kernel path (stores through the mapped address), pageable ones the
+    copy engine."""
+    if not pinned:
+        return {k: np.empty(n, np.float32) for k in NAMES}
+    torch = pytest.importorskip("torch")
+    out = {}
+    for k in NAMES:
+        t = torch.empty(n, dtype=torch.float32).pin_memory()
+        keep.append(t)
+        out[k] = t.numpy()
+    return out
+
+
+@pytest.mark.parametrize("precision,pinned", [(0, False), (1, False), (0, True), (1, True)])
+def test_async_readback_is_the_snapshot(gpu_lib, precision, pinned):
     from skewtcloudsim_gb300 import SolverConfig
     init, dt, speed = small_case((32, 32, 24))
     cfg = SolverConfig(precision=precision)
@@ -22,7 +37,8 @@ def test_async_readback_is_the_snapshot(gpu_lib, precision):
     for _ in range(3):
         a.update_gpu(dt, speed)
         want.append({k: a.read(k) for k in NAMES})
-    bufs = [{k: np.empty(b.n, np.float32) for k in NAMES} for _ in range(3)]
+    keep = []
+    bufs = [_host_buffers(b.n, pinned, keep) for _ in range(3)]
     for i in range(3):
         b.update_gpu(dt, speed)
         b.read_async(bufs[i])  # queued behind step i, copied out while step i+1 runs
