@@ -355,24 +355,26 @@ __global__ void __launch_bounds__(32 * PY) k_ppm4y(Grid g, int ylen, const float
         const float4 vm = ys >= 2 ? ld4f(vel, base + (ys - 1) * X) : make_float4(0, 0, 0, 0);  // face below y = 1 is ground: 0
         const bool oin = ys >= 3 && ys + 1 < Y;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float u = comp(vm, k);
-            setc(Fc, k, face_flux(u, comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), cdt));
-            setc(Fco, k, oin ? u : face_flux(u, orow(ys - 2), orow(ys - 1), orow(ys), orow(ys + 1), cdt));
+        for (int k = 0; k < 4; ++k) setc(Fc, k, face_flux(comp(vm, k), comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), cdt));
+        Fco = vm;  // the companion's flux is the face velocity where its window is all ones
+        if (!oin) {  // warp-uniform: a branch, not a select, so the interior skips the evaluation
+#pragma unroll
+            for (int k = 0; k < 4; ++k) setc(Fco, k, face_flux(comp(vm, k), orow(ys - 2), orow(ys - 1), orow(ys), orow(ys + 1), cdt));
         }
     }
     for (int y = ys; y < ye; ++y) {
         const float4 w4 = qrow(y + 2);
         const float4 vc = ld4f(vel, base + y * X);
         const bool oin = y >= 2 && y + 2 < Y;
-        float4 Fp, Fpo, o4;
+        float4 Fp, Fpo = vc, o4;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float u = comp(vc, k);
-            setc(Fp, k, face_flux(u, comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k), cdt));
-            setc(Fpo, k, oin ? u : face_flux(u, orow(y - 1), orow(y), orow(y + 1), orow(y + 2), cdt));
-            setc(o4, k, ppm_update(comp(w2, k), comp(Fp, k), comp(Fc, k), comp(Fpo, k), comp(Fco, k), cdt));
+        for (int k = 0; k < 4; ++k) setc(Fp, k, face_flux(comp(vc, k), comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k), cdt));
+        if (!oin) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) setc(Fpo, k, face_flux(comp(vc, k), orow(y - 1), orow(y), orow(y + 1), orow(y + 2), cdt));
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) setc(o4, k, ppm_update(comp(w2, k), comp(Fp, k), comp(Fc, k), comp(Fpo, k), comp(Fco, k), cdt));
         *reinterpret_cast<float4*>(out + base + y * X) = o4;
         Fc = Fp;
         Fco = Fpo;
@@ -422,10 +424,11 @@ __global__ void __launch_bounds__(32 * DVY) k_ppm4z(Grid g, int zlen, const floa
         }
         const bool oin = zs >= 2 && zs + 1 < Z;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float u = comp(vm, k);
-            setc(Fc, k, face_flux(u, comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), cdt));
-            setc(Fco, k, oin ? u : face_flux(u, oz(zs - 2), oz(zs - 1), oz(zs), oz(zs + 1), cdt));
+        for (int k = 0; k < 4; ++k) setc(Fc, k, face_flux(comp(vm, k), comp(w0, k), comp(w1, k), comp(w2, k), comp(w3, k), cdt));
+        Fco = vm;  // the companion's flux is the face velocity where its window is all ones
+        if (!oin) {  // warp-uniform: a branch, not a select, so the interior skips the evaluation
+#pragma unroll
+            for (int k = 0; k < 4; ++k) setc(Fco, k, face_flux(comp(vm, k), oz(zs - 2), oz(zs - 1), oz(zs), oz(zs + 1), cdt));
         }
     }
     for (int z = zs; z < ze; ++z) {
@@ -433,14 +436,15 @@ __global__ void __launch_bounds__(32 * DVY) k_ppm4z(Grid g, int zlen, const floa
         const float4 w4 = z + 2 < Z ? ld4f(in, c + 2 * XY) : (z + 1 < Z ? side4(w3) : side4(w2));
         const float4 vc = ld4f(vel, c);
         const bool oin = z >= 1 && z + 2 < Z;
-        float4 Fp, Fpo, o4;
+        float4 Fp, Fpo = vc, o4;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float u = comp(vc, k);
-            setc(Fp, k, face_flux(u, comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k), cdt));
-            setc(Fpo, k, oin ? u : face_flux(u, oz(z - 1), oz(z), oz(z + 1), oz(z + 2), cdt));
-            setc(o4, k, ppm_update(comp(w2, k), comp(Fp, k), comp(Fc, k), comp(Fpo, k), comp(Fco, k), cdt));
+        for (int k = 0; k < 4; ++k) setc(Fp, k, face_flux(comp(vc, k), comp(w1, k), comp(w2, k), comp(w3, k), comp(w4, k), cdt));
+        if (!oin) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) setc(Fpo, k, face_flux(comp(vc, k), oz(z - 1), oz(z), oz(z + 1), oz(z + 2), cdt));
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) setc(o4, k, ppm_update(comp(w2, k), comp(Fp, k), comp(Fc, k), comp(Fpo, k), comp(Fco, k), cdt));
         *reinterpret_cast<float4*>(out + c) = o4;
         Fc = Fp;
         Fco = Fpo;
