@@ -37,7 +37,7 @@ typedef enum {
     SKT_TIMEOUT = 5,
     SKT_OUT_OF_MEMORY = 6,
     SKT_NOT_INITIALIZED = 7,
-    SKT_COURANT_LIMIT = 8  /* more Courant substeps were needed than the captured step holds */
+    SKT_COURANT_LIMIT = 8  /* reserved, never returned: a step runs any substep count up to max_substeps */
 } skt_status;
 
 /* Field selector, the reference's `parameter` enum (Game/config.h:62-65) plus DENSITY. */
