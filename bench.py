@@ -61,6 +61,16 @@ STAGE_BYTES = {
 }
 
 
+# DRAM traffic per cell of one launch of the plain PCG's kernels: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch at 512x256x256 (33554432 cells), k_matvec_search4 and
+# k_residual4. Every array is streamed once per launch, so the traffic grows with the cells and is
+# scaled to the launch size here.
+MEASURED_TRAFFIC_PER_CELL = {
+    "pcg_matvec": (981.662976 + 375.963392) * 1e6 / 33554432,
+    "pcg_update": (402.723840 + 224.641536) * 1e6 / 33554432,
+}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -360,9 +370,13 @@ def main():
     roofline = None
     if bpc:
         achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
+        tpc = MEASURED_TRAFFIC_PER_CELL.get(dname) if (head["mode"] == "plain" and args.pcg_fused) else None
         roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "traffic": None, "kernel": dname,
+                    "frac": round(achieved / peak, 4), "traffic": int(tpc * cells) if tpc else None, "kernel": dname,
                     "bytes_per_cell": bpc, "launch_us": round(per_launch_ms * 1e3, 2), "peak_source": peak_kind}
+        if tpc:
+            roofline["traffic_source"] = ("ncu DRAM bytes read + written by one launch at 512x256x256, scaled to this "
+                                          "launch's cells (bytes per launch)")
     step_ms_prof = sum(v["ms"] for v in prof.values())
     bstep = step_bytes(head["mode"], head["pcg_iters"], head["outer"])
     step_model = {"bytes_per_cell_step": bstep, "achieved_gbs": round(bstep * head["value"] / 1e9, 1),
