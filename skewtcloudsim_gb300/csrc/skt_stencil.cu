@@ -894,7 +894,7 @@ namespace {
 void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float* def, float k, int sweeps) {
     const Grid& g = e.g;
     const int vx = (g.X / 4 + 31) / 32, vy = (g.Y - 1 + DVY - 1) / DVY;
-    int vz = std::max(1, std::min(g.Z, (e.num_sms * 16 + vx * vy - 1) / (vx * vy)));
+    int vz = std::max(1, std::min(g.Z, (e.num_sms * 32 + vx * vy - 1) / (vx * vy)));
     const int vlen = (g.Z + vz - 1) / vz;
     vz = (g.Z + vlen - 1) / vlen;
     float* buf[2] = {e.tA, e.tB};
