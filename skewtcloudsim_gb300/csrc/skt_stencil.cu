@@ -1023,7 +1023,7 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     const dim3 vg2(gx, gy, zc2);
     // the Y pass marches rows in runs
     const int ygz = (g.Z + PY - 1) / PY;
-    int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * 16 + gx * ygz - 1) / (gx * ygz)));
+    int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * 32 + gx * ygz - 1) / (gx * ygz)));
     const int ylen = (g.Y - 1 + yc - 1) / yc;
     yc = (g.Y - 1 + ylen - 1) / ylen;
     const dim3 yg(gx, ygz, yc), yb(32, PY);
