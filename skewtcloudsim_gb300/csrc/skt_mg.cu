@@ -1165,7 +1165,7 @@ void vcycle_vec(Env& e, int l, const CT* ax, const CT* ay, const CT* az, const C
 void mg_solve(Env& e) {
     const Grid& g = e.g;
     const int n = g.N;
-    const int nb = std::min((n + RT - 1) / RT, std::min(e.num_sms * 8, kMaxPartials));
+    const int nb = std::min((n + RT - 1) / RT, std::min(e.num_sms * 16, kMaxPartials));
     float* bvec = e.tA;
     float* ecor = e.tB;
     float* z0 = (float*)e.rd;

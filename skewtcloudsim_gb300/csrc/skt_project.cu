@@ -928,9 +928,11 @@ void launch_project(Env& e, float dtS) {
     } else {
     const int chunk = 8;
     const bool vec = (g.X % 4) == 0;
-    // vectorised launch shapes: streams at 8 blocks/SM, the matvec's z chunks sized to fill the GPU
+    // vectorised launch shapes: streams at 16 blocks/SM (several waves of the grid-stride loop:
+    // 8 per SM, 1.3 waves, left the second wave a third full), the matvec's z chunks sized to fill
+    // the GPU
     const int n4 = g.N / 4;
-    const int nstream = std::min(std::min((n4 + UT - 1) / UT, e.num_sms * 8), kMaxPartials);
+    const int nstream = std::min(std::min((n4 + UT - 1) / UT, e.num_sms * 16), kMaxPartials);
     const dim3 mvb(32, MVY);
     const int gx = (g.X / 4 + 31) / 32, gy = (g.Y + MVY - 1) / MVY;
     int zc = std::max(1, std::min(g.Z, (e.num_sms * 8 + gx * gy - 1) / (gx * gy)));
