@@ -259,10 +259,15 @@ __global__ void __launch_bounds__(32 * DVY, 32 / DVY) k_ppm4x(Grid g, int zlen, 
     const float dy = wact ? (def ? def[y] : 0.0f) : 0.0f;
     const float du = wact ? defU[y] : 0.0f;
     const float so = bc_val(sides, 1.0f, 1.0f);
-    const bool xedge = x0 < 4 || x0 + 8 > X;  // the companion window reaches outside the domain
     const bool xedge0 = xw < 4 || xw + 8 > X;
-    auto ow = [&](int j) { return (x0 - 2 + j >= 0 && x0 - 2 + j < X) ? 1.0f : so; };
     auto ow0 = [&](int j) { return (xw - 2 + j >= 0 && xw - 2 + j < X) ? 1.0f : so; };
+    // The density companion's window reaches outside the domain only for the cells x0 = 0 (lane 0
+    // of the first warp of a row) and x0 = X - 4 (one lane of the last warp); elsewhere its flux
+    // is the face velocity. Those lanes' four companion fluxes are formed in the 32-plane batch,
+    // one plane per lane, and handed to the edge lane plane by plane (warp-uniform branches).
+    const int xr = X - 4, lr = (xr - xw) >> 2;
+    const bool has_l = wact && xw == 0, has_r = wact && xr >= xw && xr < xw + 128;
+    auto owx = [&](int xe, int j) { return (xe - 2 + j >= 0 && xe - 2 + j < X) ? 1.0f : so; };
     for (int zb = zs; zb < ze; zb += 32) {
         // the warp's lower boundary face for planes zb .. zb+31: plane zb + lane on this lane
         float Bq = 0.0f, BF = 0.0f, BFo = 0.0f;
@@ -274,6 +279,20 @@ __global__ void __launch_bounds__(32 * DVY, 32 / DVY) k_ppm4x(Grid g, int zlen, 
             else { a0 = Bq = bc_val(sides, a2, dy); um = bc_val(sides, vel[cw], du); }
             BF = face_flux(um, a0, Bq, a2, a3, cdt);
             BFo = xedge0 ? face_flux(um, ow0(0), ow0(1), ow0(2), ow0(3), cdt) : um;
+        }
+        float4 EL = make_float4(0, 0, 0, 0), ER = EL;  // the edge lanes' companion fluxes, plane zb + lane
+        if ((has_l || has_r) && zb + lane < ze) {
+            const int pz = y * X + (zb + lane) * XY;
+            if (has_l) {
+                const float4 ue = ld4f(vel, pz);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) setc(EL, k, face_flux(comp(ue, k), owx(0, k + 1), owx(0, k + 2), owx(0, k + 3), owx(0, k + 4), cdt));
+            }
+            if (has_r) {
+                const float4 ue = ld4f(vel, pz + xr);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) setc(ER, k, face_flux(comp(ue, k), owx(xr, k + 1), owx(xr, k + 2), owx(xr, k + 3), owx(xr, k + 4), cdt));
+            }
         }
         const int zend = min(zb + 32, ze);
         for (int z = zb; z < zend; ++z) {
@@ -299,9 +318,19 @@ __global__ void __launch_bounds__(32 * DVY, 32 / DVY) k_ppm4x(Grid g, int zlen, 
                 F[k] = face_flux(u[k], w[k], w[k + 1], w[k + 2], w[k + 3], cdt);
                 Fo[k] = u[k];
             }
-            if (xedge) {
+            if (has_l) {
 #pragma unroll
-                for (int k = 0; k < 4; ++k) Fo[k] = face_flux(u[k], ow(k + 1), ow(k + 2), ow(k + 3), ow(k + 4), cdt);
+                for (int k = 0; k < 4; ++k) {
+                    const float v = __shfl_sync(0xffffffffu, comp(EL, k), src);
+                    if (lane == 0) Fo[k] = v;
+                }
+            }
+            if (has_r) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float v = __shfl_sync(0xffffffffu, comp(ER, k), src);
+                    if (lane == lr) Fo[k] = v;
+                }
             }
             float Fm = __shfl_up_sync(0xffffffffu, F[3], 1);
             float Fmo = __shfl_up_sync(0xffffffffu, Fo[3], 1);
