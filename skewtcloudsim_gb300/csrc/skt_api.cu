@@ -156,6 +156,23 @@ skt_status check_cuda(Env& e, const char* where) { return cuda_check(e, where); 
 __global__ void k_fetch_sc(const unsigned* __restrict__ src, unsigned* dst, int nwords) {
     for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
 }
+// AoS (u, v, w per cell, Game/environment.cu:263-281) to the three SoA fields on the device. The
+// AoS array of 3n floats arrives in three pieces of n floats (float f of the array is float
+// f % n of piece f / n).
+__global__ void k_aos_to_soa(size_t n, const float* __restrict__ p0, const float* __restrict__ p1, const float* __restrict__ p2,
+                             float* __restrict__ u, float* __restrict__ v, float* __restrict__ w) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        float out[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const size_t f = 3 * i + c, piece = f / n, off = f - piece * n;
+            out[c] = (piece == 0 ? p0 : (piece == 1 ? p1 : p2))[off];
+        }
+        u[i] = out[0];
+        v[i] = out[1];
+        w[i] = out[2];
+    }
+}
 __global__ void k_snapshot(const float4* __restrict__ src, float4* __restrict__ dst, size_t n4) {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n4; i += size_t(gridDim.x) * blockDim.x) dst[i] = src[i];
 }
@@ -390,17 +407,14 @@ skt_status skt_init(skt_env* env, const float* theta, const float* vel, const fl
     int flat = 1;
     for (size_t i = 0; i < NG; ++i) flat &= gh[i] == 0;
     e.flat = flat;
-    // AoS -> SoA (Game/environment.cu:263-281)
-    std::vector<float> u(N), v(N), w(N);
-    for (size_t i = 0; i < N; ++i) {
-        u[i] = vel[3 * i];
-        v[i] = vel[3 * i + 1];
-        w[i] = vel[3 * i + 2];
-    }
+    // AoS -> SoA (Game/environment.cu:263-281) on the device: the velocity array is copied as it
+    // is, in three pieces, into scratch fields that are free before the first step
+    float* piece[3] = {e.tA, e.tB, e.As};
+    for (int j = 0; j < 3; ++j) cudaMemcpyAsync(piece[j], vel + size_t(j) * N, N * 4, cudaMemcpyHostToDevice, e.stream);
+    k_aos_to_soa<<<int(std::min<size_t>((N + 255) / 256, size_t(e.num_sms) * 16)), 256, 0, e.stream>>>(N, piece[0], piece[1], piece[2],
+                                                                                                    e.u, e.v, e.w);
+    e.launches += 1;
     cudaMemcpyAsync(e.th, theta, N * 4, cudaMemcpyHostToDevice, e.stream);
-    cudaMemcpyAsync(e.u, u.data(), N * 4, cudaMemcpyHostToDevice, e.stream);
-    cudaMemcpyAsync(e.v, v.data(), N * 4, cudaMemcpyHostToDevice, e.stream);
-    cudaMemcpyAsync(e.w, w.data(), N * 4, cudaMemcpyHostToDevice, e.stream);
     cudaMemcpyAsync(e.qv, qv, N * 4, cudaMemcpyHostToDevice, e.stream);
     cudaMemcpyAsync(e.Tg, ground_T, NG * 4, cudaMemcpyHostToDevice, e.stream);
     cudaMemcpyAsync(e.Pg, ground_p, NG * 4, cudaMemcpyHostToDevice, e.stream);
