@@ -177,7 +177,7 @@ __global__ void k_snapshot(const float4* __restrict__ src, float4* __restrict__ 
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n4; i += size_t(gridDim.x) * blockDim.x) dst[i] = src[i];
 }
 
-constexpr int kHostCopyBlocks = 64;  // blocks of the kernel that writes a snapshot to mapped host memory
+constexpr int kHostCopyBlocks = 32;  // blocks of the kernel that writes a snapshot to mapped host memory (176 GB/s alone)
 
 void fetch_scalars(Env& e) {
     static_assert(sizeof(Scalars) % 4 == 0, "Scalars is copied as 32-bit words");
