@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(UT) k_search4(int n4, const float4* __restrict
     }
 }
 
-constexpr int MVY = 16;           // y rows per block (neighbour rows of s mostly from L1)
+constexpr int MVY = 32;           // y rows per block (neighbour rows of s mostly from L1)
 constexpr int MVT = 32 * MVY;     // threads per block
 
 __device__ __forceinline__ float4 ld4(const float* p, int c) { return *reinterpret_cast<const float4*>(p + c); }
