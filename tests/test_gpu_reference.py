@@ -44,8 +44,9 @@ def _grids():
 
 
 def _record(name, data):
-    d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
-    if os.path.isdir(d):
+    """Writes the per-step distances to $SKT_REPORT_DIR/refparity_<grid>.json when that folder is set."""
+    d = os.environ.get("SKT_REPORT_DIR", "")
+    if d and os.path.isdir(d):
         with open(os.path.join(d, f"refparity_{name}.json"), "w") as f:
             json.dump(data, f, indent=1)
 
