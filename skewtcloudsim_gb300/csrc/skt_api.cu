@@ -374,7 +374,6 @@ void skt_destroy(skt_env* env) {
     if (!env) return;
     Env& e = env->e;
     if (e.stream) cudaStreamSynchronize(e.stream);
-    if (e.graph_exec) cudaGraphExecDestroy(e.graph_exec);
     if (e.ev0) cudaEventDestroy(e.ev0);
     if (e.ev1) cudaEventDestroy(e.ev1);
     if (e.pool) cudaFree(e.pool);

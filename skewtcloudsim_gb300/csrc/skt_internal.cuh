@@ -156,8 +156,6 @@ struct Env {
     std::string err;
     int flat = 1;  // all gh == 0
     // graph
-    cudaGraphExec_t graph_exec = nullptr;
-    float graph_dt = 0.0f, graph_speed = 0.0f;
     // multigrid hierarchy of the mixed-precision solve (level 0 = the grid itself)
     int mg_levels = 0;
     void* mg_pool = nullptr;
