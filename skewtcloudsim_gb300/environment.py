@@ -149,8 +149,9 @@ class Environment:
     # -- lifetime --------------------------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None):
-            self._L.skt_destroy(self._h)
+            self._L.skt_destroy(self._h)  # waits for pending readback copies first
             self._h = None
+        self._pending_reads = None
 
     def __del__(self):
         try:
@@ -216,7 +217,7 @@ class Environment:
     def read_async(self, outs: dict):
         """skt_read_fields_async: queue the readback of the fields named in ``outs`` (name -> float32
         array of n values, ideally pinned) as they stand after the queued work; returns at once.
-        The arrays must stay alive until ``read_wait``."""
+        The arrays of every call are kept alive here until ``read_wait``."""
         names = list(outs)
         prm = (ctypes.c_int * len(names))(*[int(FIELDS[k][0]) for k in names])
         drs = (ctypes.c_int * len(names))(*[int(FIELDS[k][1]) for k in names])
@@ -225,7 +226,9 @@ class Environment:
             if a.dtype != np.float32 or a.size != self.n or not a.flags.c_contiguous:
                 raise ValueError(f"{k}: need a contiguous float32 array of {self.n} values")
         dst = (_lib.c_float_p * len(names))(*[_fp(outs[k]) for k in names])
-        self._pending_reads = outs  # keep the buffers alive until read_wait
+        if getattr(self, "_pending_reads", None) is None:
+            self._pending_reads = []
+        self._pending_reads.append(outs)  # the device may still write them after this call returns
         self._check(self._L.skt_read_fields_async(self._h, len(names), prm, drs, dst, self.n))
 
     def read_wait(self):
