@@ -69,6 +69,16 @@ public:
         return out;
     }
 
+    // the per-step readback without waiting: the fields as they stand after the queued step are
+    // written to dst[i] (n floats each; pinned buffers for overlap) while the next steps run;
+    // the buffers must stay valid until readWait()
+    void readFieldsAsync(const std::vector<skt_param>& params, const std::vector<skt_direction>& dirs, float* const* dst) {
+        std::vector<int> p(params.begin(), params.end()), d(dirs.begin(), dirs.end());
+        if (d.size() != p.size()) throw Error(SKT_INVALID_ARG, "one direction per field");
+        check(skt_read_fields_async(env_, int(p.size()), p.data(), d.data(), dst, n_));
+    }
+    void readWait() { check(skt_read_wait(env_)); }
+
     skt_step_stats stats() {
         skt_step_stats s{};
         check(skt_stats(env_, &s));
