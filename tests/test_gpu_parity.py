@@ -272,3 +272,25 @@ def test_projection_fused_iteration_matches_three_launch(gpu_lib, sem, terrain):
     m = st.sky_mask()
     for k in ("u", "v", "w", "p"):
         assert rel_l2(got[1][1][k], got[0][1][k], m) <= STEP_TOL, k
+
+
+@pytest.mark.parametrize("cap", [1, 6, 7])
+def test_projection_fused_iteration_at_the_cap(gpu_lib, cap):
+    """The fused iteration stopped by the iteration cap after an odd or even number of iterations
+    (the last direction sits in either buffer, and its pressure update is applied after the
+    loop): the same pressure and winds as the three-launch iteration with the same cap."""
+    init, dt, speed = small_case(SHAPE)
+    st0 = oracle.OracleState(init, np.float32)
+    for _ in range(2):
+        st0.step(oracle_cfg(), dt, speed)
+    got = {}
+    for fused in (1, 0):
+        env = make_env(init, gpu_cfg(0, pcg_fused=fused, pcg_max_iter=cap))
+        push_oracle_to_env(st0, env)
+        g = env.run_stage(3, 0, dt * speed)
+        assert g["pcg_iters"] == cap and not g["converged"], g
+        got[fused] = {k: env.read(k) for k in ("u", "v", "w", "p")}
+        env.close()
+    m = st0.sky_mask()
+    for k in ("u", "v", "w", "p"):
+        assert rel_l2(got[1][k], got[0][k], m) <= 1e-6, k
