@@ -141,7 +141,9 @@ skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float
  * dir selects the wind component for SKT_WIND. n must equal nx*ny*nz. Synchronous. */
 skt_status skt_read_field(skt_env* env, int param, int dir, float* host_dst, size_t n);
 
-/* Asynchronous readback of several fields (same selectors): the fields as they stand after the
+/* The per-frame readback of editor::GPUSetEnv (Game/editor.cpp:226-260, all 11 sky fields after
+ * every step), without stalling the step loop.
+ * Asynchronous readback of several fields (same selectors): the fields as they stand after the
  * work queued so far are snapshot on the device, then copied to host_dsts[i] on a second stream,
  * so that the next steps can run while the copies proceed; the call returns at once. A new
  * snapshot first waits for the previous one's copies. The host buffers (n floats each, n =
