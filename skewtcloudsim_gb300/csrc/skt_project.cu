@@ -883,6 +883,61 @@ __global__ void __launch_bounds__(256) k_apply_proj(Grid g, const float* __restr
     w[c] += (pf - cp) / df;
 }
 
+// k_apply_proj for flat terrain and X % 4 == 0: four cells per thread and a march along z over the
+// sky rows (the next plane's pressure correction and density are the front neighbours and become
+// the next step's own values); each cell's reciprocal density is formed once. Flat ground is
+// the row y = 0, so the +x, +y and +z neighbours of a sky cell are never ground: outside the
+// domain the correction is 0 (DIRICHLET) and the density the cell's own (NEUMANN). Same
+// arithmetic as k_apply_proj.
+__global__ void __launch_bounds__(256) k_apply_proj4(Grid g, int zlen, const float* __restrict__ pp, const float* __restrict__ rho,
+                                                     float* __restrict__ u, float* __restrict__ v, float* __restrict__ w) {
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * 8 + threadIdx.y + 1;  // sky rows start at y = 1
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const bool act = x0 < g.X && y < g.Y;
+    const int X = g.X, XY = g.XY;
+    const int row = x0 + y * X;
+    float4 pc = f4zero(), dc = f4zero();
+    if (act) {
+        pc = ld4(pp, row + zs * XY);
+        dc = ld4(rho, row + zs * XY);
+    }
+    for (int z = zs; z < ze; ++z) {
+        const int c = row + z * XY;
+        float4 pf = f4zero(), df = dc, pu = f4zero(), du = dc;
+        if (act) {
+            if (z + 1 < g.Z) { pf = ld4(pp, c + XY); df = ld4(rho, c + XY); }
+            if (y + 1 < g.Y) { pu = ld4(pp, c + X); du = ld4(rho, c + X); }
+        }
+        float pr3 = __shfl_down_sync(0xffffffffu, pc.x, 1), dr3 = __shfl_down_sync(0xffffffffu, dc.x, 1);
+        if (act && (lane == 31 || x0 + 4 >= X)) {
+            if (x0 + 4 < X) { pr3 = pp[c + 4]; dr3 = rho[c + 4]; }
+            else { pr3 = 0.0f; dr3 = dc.w; }
+        }
+        if (act) {
+            const float prx[4] = {pc.y, pc.z, pc.w, pr3}, drx[4] = {dc.y, dc.z, dc.w, dr3};
+            float4 uo = ld4(u, c), vo = ld4(v, c), wo = ld4(w, c);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float cp = fcomp(pc, k), cd = fcomp(dc, k), rc = 1.0f / cd;
+                float dr = drx[k], dU = fcomp(du, k), dF = fcomp(df, k);
+                dr = dr == 0.0f ? cd : 2.0f / (rc + 1.0f / dr);
+                dU = dU == 0.0f ? cd : 2.0f / (rc + 1.0f / dU);
+                dF = dF == 0.0f ? cd : 2.0f / (rc + 1.0f / dF);
+                fset(uo, k, fcomp(uo, k) + (prx[k] - cp) / dr);
+                fset(vo, k, fcomp(vo, k) + (fcomp(pu, k) - cp) / dU);
+                fset(wo, k, fcomp(wo, k) + (fcomp(pf, k) - cp) / dF);
+            }
+            *reinterpret_cast<float4*>(u + c) = uo;
+            *reinterpret_cast<float4*>(v + c) = vo;
+            *reinterpret_cast<float4*>(w + c) = wo;
+        }
+        pc = pf;
+        dc = df;
+    }
+}
+
 }  // namespace
 
 // As = A s and s.As -> alpha (textbook operator, vectorised; X % 4 == 0)
@@ -999,7 +1054,15 @@ void launch_project(Env& e, float dtS) {
     ProfScope ps(e, "proj_apply");
     e.launches += 2;
     k_press_dens<<<grd, blk, 0, e.stream>>>(g, e.p, e.pp, e.rho, e.th, e.qv, e.Pg);
-    k_apply_proj<<<grd, blk, 0, e.stream>>>(g, e.pp, e.rho, e.u, e.v, e.w);
+    if (e.flat && (g.X % 4) == 0) {
+        const int ax = (g.X / 4 + 31) / 32, ay = (g.Y - 1 + 7) / 8;
+        int az = std::max(1, std::min(g.Z, (e.num_sms * 16 + ax * ay - 1) / (ax * ay)));
+        const int alen = (g.Z + az - 1) / az;
+        az = (g.Z + alen - 1) / alen;
+        k_apply_proj4<<<dim3(ax, ay, az), dim3(32, 8), 0, e.stream>>>(g, alen, e.pp, e.rho, e.u, e.v, e.w);
+    } else {
+        k_apply_proj<<<grd, blk, 0, e.stream>>>(g, e.pp, e.rho, e.u, e.v, e.w);
+    }
 }
 
 }  // namespace skt

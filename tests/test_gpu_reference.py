@@ -69,9 +69,10 @@ def test_step_against_reference_kernels(gpu_lib, grid):
         m = ref.sky_mask()
         finite = all(np.isfinite(ref.a[k][m]).all() for k in SKY)
         # the reference reads uninitialised shared memory at interior ground-tile edges (grids
-        # wider than 16): its state turns NaN, or stays finite but wrong; the independent oracle
-        # tells the two apart (it agrees with the reference to ~1e-6 whenever the reference is sound)
-        sound = finite and all(rel_l2(orc.a[k], ref.a[k], m) <= 1e-3 for k in SKY)
+        # wider than 16): its state turns NaN, or stays finite but wrong, by anything from a few
+        # 1e-5 to O(1) and differently from run to run; the independent oracle tells the two apart
+        # (it agrees with the reference to ~1e-6 whenever the reference is sound)
+        sound = finite and all(rel_l2(orc.a[k], ref.a[k], m) <= 1e-5 for k in SKY)
         row = {"ref_finite": bool(finite), "ref_sound": bool(sound), "step": step + 1, "ref_pcg": rd["pcg_iters"][0], "oracle_pcg": od["pcg_iters"], "gpu_pcg": gd["pcg_iters"],
                "nsub_ref": rd["nsub"][0], "nsub_gpu": gd["nsub"]}
         for k in SKY:
