@@ -93,3 +93,22 @@ def test_cpp_adapter_compiles_and_links(tmp_path):
                     f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0 and out.stdout.startswith("skewt-gb300")
+
+
+def test_c_header_compiles_as_strict_c(tmp_path):
+    """include/skewt.h is a C header: a C11 program (-Wall -Wextra -pedantic -Werror) includes it,
+    links libskewt_gb300.so and reads the default configuration (no GPU work)."""
+    import subprocess
+    from skewtcloudsim_gb300 import build
+    lib = build.build()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "use_abi.c"
+    src.write_text('#include "skewt.h"\n#include <stdio.h>\n'
+                   'int main(void) { skt_solver_cfg c; skt_default_config(&c);'
+                   ' printf("%s %d\\n", skt_version(), c.pcg_fused); return c.pcg_max_iter == 200 ? 0 : 1; }\n')
+    exe = tmp_path / "use_abi"
+    libdir = os.path.dirname(lib)
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", str(src), "-I", os.path.join(root, "include"),
+                    "-L", libdir, "-lskewt_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.startswith("skewt-gb300") and out.stdout.strip().endswith("1")
