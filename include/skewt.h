@@ -33,8 +33,8 @@ typedef enum {
     SKT_INVALID_ARG = 1,
     SKT_CUDA_ERROR = 2,
     SKT_NOT_CONVERGED = 3, /* the PCG hit its iteration cap; the step still completed */
-    SKT_NAN_DETECTED = 4,
-    SKT_TIMEOUT = 5,
+    SKT_NAN_DETECTED = 4,  /* a step met a NaN or Inf (wind maximum or pressure-solver reduction); stepping stopped */
+    SKT_TIMEOUT = 5,       /* reserved, never returned: no kernel here waits on another */
     SKT_OUT_OF_MEMORY = 6,
     SKT_NOT_INITIALIZED = 7,
     SKT_COURANT_LIMIT = 8  /* reserved, never returned: a step runs any substep count up to max_substeps */
@@ -120,7 +120,10 @@ skt_status skt_init(skt_env* env, const float* theta, const float* vel_aos3, con
 
 /* Replaces environmentGPU::updateGPU(dt, speed) (Game/environment.cu:391-555), nsteps times.
  * Returns SKT_NOT_CONVERGED when a projection hit its iteration cap (the step is still done, as
- * in the reference). Does not read fields back (the reference's per-step GPUSetEnv copy,
+ * in the reference). Returns SKT_NAN_DETECTED when a step met a NaN or Inf: the Courant wind
+ * maximum saw a non-finite wind, or a dot product of the pressure solve came out non-finite (a
+ * non-finite field value or a zero-density cell reaches it within the step); the steps after it
+ * are not run and the fields are not valid (the reference runs on with NaNs). Does not read fields back (the reference's per-step GPUSetEnv copy,
  * Game/environment.cu:553, is explicit here: skt_read_field). */
 skt_status skt_step(skt_env* env, float dt, float speed, int nsteps);
 
@@ -196,8 +199,14 @@ skt_status skt_profile_read(skt_env* env, char* buf, size_t n);
  * caller-owned device buffers: in_dev is read, out_dev receives the result (ground cells copied
  * from in_dev). The one intermediate buffer lives in a static device array of
  * SKT_NOALLOC_MAX_CELLS floats (8 MiB) that every GPU loading the library holds until exit;
- * larger grids are rejected with SKT_INVALID_ARG (message in skt_last_error(NULL)). The first
- * call on each device looks up that array's address, so make it before any stream capture.
+ * larger grids are rejected with SKT_INVALID_ARG (message in skt_last_error(NULL)), as are
+ * nz > 65535 and ny > 524280 (CUDA grid limits). The first call in each CUDA context (a device's
+ * primary context, or a driver-API context the caller made current) looks up that array's address,
+ * so make it before any stream capture, with the context the later calls will use current.
+ * Buffers: in_dev and out_dev hold nx*ny*nz floats, ground_height_dev, ground_T_dev and
+ * ground_p_dev nx*nz values, default_column_dev ny floats (the level defaults of this field type:
+ * the isentrope for theta and Qv, the default u or w column for u and w; unused for types 3 and 5,
+ * may be NULL there), p_dev nx*ny*nz floats (theta only; the others may pass NULL).
  * Calls share the array: calls whose work overlaps on the GPU race. Work is queued on `stream`
  * (a cudaStream_t; NULL = default stream); the call does not synchronise. Nothing in the array
  * needs clearing between calls (every value is written before it is read). */
@@ -260,6 +269,15 @@ skt_status skt_apply_selection(skt_env* env, int param, const int lo[3], const i
  * first ground cell, as the reference's setToDefault does), v and Qw..Qi to 0 everywhere.
  * Synchronous. */
 skt_status skt_reset_parameter(skt_env* env, int param);
+
+/* The boundary class of every cell's six neighbours as the library's kernels derive it from the
+ * heightfield, written as the reference's Neigh records (computeNeighbourGPU,
+ * Game/kernelSky.cu:1284-1316, which the reference stores per cell and this library does not):
+ * 12 bytes per cell, for left (-x), right (+x), up (+y), down (-y), forward (+z), backward (-z)
+ * a byte `outside` (the neighbour lies outside the grid) and a byte `type` (0 sky, 1 ground).
+ * n is the cell count nx*ny*nz; host_dst holds 12*n bytes. Allocates a temporary device buffer.
+ * Synchronous. */
+skt_status skt_read_neighbours(skt_env* env, uint8_t* host_dst, size_t n);
 
 /* The current heightfield (nx*nz values). Synchronous. */
 skt_status skt_read_ground_height(skt_env* env, int32_t* host_dst, size_t n);

@@ -92,6 +92,9 @@ def lib():
         L.oc_reset_parameter_f32.restype = ctypes.c_int
         L.oc_editor_block_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OcState)]
         L.oc_editor_block_f32.restype = ctypes.c_int
+        L.oc_projection_residual_f32.argtypes = [ctypes.POINTER(OcConfig), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(OcState), FP, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]
+        L.oc_projection_residual_f32.restype = ctypes.c_int
         L.oc_irradiance.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
         L.oc_irradiance.restype = ctypes.c_float
         L.oc_num_threads.restype = ctypes.c_int
@@ -188,6 +191,19 @@ class OracleState:
         if rc != 0:
             raise RuntimeError(f"oracle stage failed: {rc}")
         return {"pcg_iters": d.pcg_iters, "pcg_residual": d.pcg_residual, "nsub": d.nsub[0]}
+
+    def projection_residual(self, cfg: Config, pp, dt: float):
+        """For a pressure correction ``pp`` (FP32), the residual of the projection's linear system
+        built from this (FP32) state as the projection stage builds it: (max |r - A pp|,
+        ||r - A pp||_2, max |r|, ||r||_2) over sky cells. The state is not changed."""
+        assert self.dtype == np.float32
+        st = self._cstate()
+        p = np.ascontiguousarray(pp, np.float32)
+        out = (ctypes.c_double * 4)()
+        c = cfg.c(self.voxel)
+        lib().oc_projection_residual_f32(ctypes.byref(c), self.X, self.Y, self.Z, ctypes.byref(st),
+                                         p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), dt, out)
+        return tuple(out[:])
 
     def micro_rates(self, dt: float, speed: float, lo, hi):
         """The microphysics stage (FP32 state) and the 33 region-summed process amounts."""

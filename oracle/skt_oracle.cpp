@@ -249,6 +249,7 @@ void ppm_pass(const Grid& g, const State<T>& s, int axis, const T* q, T* out, co
 // the integer atomicMax; TEXTBOOK: max |a|.
 template <class T> double quirky_max(const Grid& g, const T* a, bool reference) {
     double m = 0;
+#pragma omp parallel for schedule(static) reduction(max : m)
     for (int z = 0; z < g.Z; ++z)
         for (int y = 0; y < g.Y; ++y)
             for (int x = 0; x < g.X; ++x) {
@@ -472,8 +473,10 @@ template <class T> inline T char_trunc(T a) {  // (char) conversion of a float, 
     return t;
 }
 
+// The projection's linear system A p = r: resetVelPressProj on the winds, the matrix of
+// initAMatrix and the divergence of calculateDivergenceGPU (r), as pressureProject sets them up.
 template <class T>
-double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
+void build_system(const Grid& g, const Config& cfg, State<T>& s, T dt, Amat<T>& A, std::vector<T>& r) {
     const bool ref = cfg.semantics == 0;
     const int64_t N = g.n();
     // resetVelPressProj :1648-1682 (REFERENCE: stop the column at the first ground z, Q8)
@@ -490,7 +493,6 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
             }
     // initAMatrix :1320-1393 with bounds {NEUMANN sides, DIRICHLET ground}
     const Bounds bA{NEUMANN, DIRICHLET};
-    Amat<T> A;
     A.x.assign(N, 0); A.y.assign(N, 0); A.z.assign(N, 0); A.w.assign(N, 0);
 #pragma omp parallel for collapse(2) schedule(static)
     for (int z = 0; z < g.Z; ++z)
@@ -512,7 +514,7 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
     // calculateDivergenceGPU :780-860; densities {NEUMANN sides, DIRICHLET ground}, velocities
     // m_boundsVelX = {CUSTOM sides, DIRICHLET ground}
     const Bounds bD{NEUMANN, DIRICHLET}, bV{CUSTOM, DIRICHLET};
-    std::vector<T> r(N, 0), zv(N, 0), sv(N, 0), As(N, 0), pp(N, 0);
+    r.assign(N, 0);
     std::vector<T> oldrho(s.rho, s.rho + N);
 #pragma omp parallel for collapse(2) schedule(static)
     for (int z = 0; z < g.Z; ++z)
@@ -535,15 +537,36 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
                 const T dch = (cur - oldrho[idx]) / dt;
                 r[idx] = mfd - dch;
             }
+}
+
+template <class T>
+double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
+    const bool ref = cfg.semantics == 0;
+    const int64_t N = g.n();
+    Amat<T> A;
+    std::vector<T> r;
+    build_system(g, cfg, s, dt, A, r);
+    std::vector<T> zv(N, 0), sv(N, 0), As(N, 0), pp(N, 0);
     // Jacobi preconditioner (initPrecon :1395) and the PCG loop (:898-987)
     auto precon = [&](int64_t i) { return A.w[i] == T(0) ? T(1) : T(1) / A.w[i]; };
     auto is_sky = [&](int64_t i, int& x, int& y, int& z) {
         x = int(i % g.X); y = int((i / g.X) % g.Y); z = int(i / (int64_t(g.X) * g.Y));
         return !g.ground(x, y, z);
     };
+    // dot products over sky cells in double: kDotChunks fixed chunks summed in parallel, then the
+    // chunk sums added in chunk order, so the result does not depend on the thread count
+    constexpr int kDotChunks = 256;
     auto dot = [&](const std::vector<T>& a, const std::vector<T>& b) {
+        double part[kDotChunks];
+#pragma omp parallel for schedule(static)
+        for (int ch = 0; ch < kDotChunks; ++ch) {
+            const int64_t i0 = N * ch / kDotChunks, i1 = N * (ch + 1) / kDotChunks;
+            double acc = 0;
+            for (int64_t i = i0; i < i1; ++i) { int x, y, z; if (is_sky(i, x, y, z)) acc += double(a[i]) * double(b[i]); }
+            part[ch] = acc;
+        }
         double acc = 0;
-        for (int64_t i = 0; i < N; ++i) { int x, y, z; if (is_sky(i, x, y, z)) acc += double(a[i]) * double(b[i]); }
+        for (int ch = 0; ch < kDotChunks; ++ch) acc += part[ch];
         return acc;
     };
     auto applyA = [&](const std::vector<T>& in, std::vector<T>& out) {  // applyAGPU :719-778, ghost s = 0
@@ -575,6 +598,7 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
     dg.converged = 1;
     double res = mr;
     if (mr != 0.0) {
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < N; ++i) { int x, y, z; zv[i] = is_sky(i, x, y, z) ? r[i] * precon(i) : T(0); }
         sv = zv;
         double sigma0 = dot(zv, r);
@@ -585,6 +609,7 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
             const double sAs = dot(As, sv);
             sigma1 = ref ? sigma1 + sAs : sAs;  // Q1: the reference never clears sigma1 here
             const T alpha = T(sigma0 / sigma1);
+#pragma omp parallel for schedule(static)
             for (int64_t i = 0; i < N; ++i) {
                 int x, y, z;
                 if (!is_sky(i, x, y, z)) continue;
@@ -595,9 +620,11 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
             mr = maxr();
             res = mr;
             if (mr <= double(T(cfg.pcg_tol))) { dg.converged = 1; break; }
+#pragma omp parallel for schedule(static)
             for (int64_t i = 0; i < N; ++i) { int x, y, z; zv[i] = is_sky(i, x, y, z) ? r[i] * precon(i) : T(0); }
             sigma1 = dot(zv, r);
             const T beta = T(sigma1 / sigma0);
+#pragma omp parallel for schedule(static)
             for (int64_t i = 0; i < N; ++i) {
                 int x, y, z;
                 if (!is_sky(i, x, y, z)) continue;
@@ -610,7 +637,7 @@ double project(const Grid& g, const Config& cfg, State<T>& s, T dt, Diag& dg) {
     // updatePressure :1016, initDensity, applyPresProjGPU :862-908
     for (int64_t i = 0; i < N; ++i) { int x, y, z; if (is_sky(i, x, y, z)) s.p[i] -= pp[i] / T(100); }
     init_density(g, s);
-    const Bounds bP{DIRICHLET, NEUMANN};
+    const Bounds bP{DIRICHLET, NEUMANN}, bD{NEUMANN, DIRICHLET};
 #pragma omp parallel for collapse(2) schedule(static)
     for (int z = 0; z < g.Z; ++z)
         for (int y = 0; y < g.Y; ++y)
@@ -1371,6 +1398,53 @@ int oc_stage_f32(const oc_config* c, int X, int Y, int Z, oc_state* st, int stag
 }
 int oc_stage_f64(const oc_config* c, int X, int Y, int Z, oc_state* st, int stage, int arg, float dt, float speed, oc_diag* d) {
     return stage_impl<double>(c, X, Y, Z, st, stage, arg, dt, speed, d);
+}
+
+// The residual r - A pp of the projection's linear system for a given pressure correction pp:
+// A and r are built in float from the state as the projection stage (density, then
+// pressureProject's set-up) builds them; the products and the residual are formed in double.
+// The state is not modified. out: max |r - A pp| and its L2 norm over sky cells, then max |r| and
+// its L2 norm (the divergence before the projection).
+int oc_projection_residual_f32(const oc_config* c, int X, int Y, int Z, const oc_state* st, const float* pp, float dt, double* out) {
+    State<float> s = unpack<float>(st);
+    Grid g{X, Y, Z, s.gh};
+    Config cf = cfg_of(c);
+    const int64_t N = g.n();
+    std::vector<float> u(s.u, s.u + N), v(s.v, s.v + N), w(s.w, s.w + N), rho(s.rho, s.rho + N);
+    s.u = u.data(); s.v = v.data(); s.w = w.data(); s.rho = rho.data();
+    init_density(g, s);
+    Amat<float> A;
+    std::vector<float> r;
+    build_system(g, cf, s, dt, A, r);
+    const bool ref = cf.semantics == 0;
+    double mx = 0, l2 = 0, bmx = 0, bl2 = 0;
+    for (int z = 0; z < Z; ++z)
+        for (int y = 0; y < Y; ++y)
+            for (int x = 0; x < X; ++x) {
+                if (g.ground(x, y, z)) continue;
+                const int64_t idx = g.id(x, y, z);
+                auto S = [&](int dx, int dy, int dz) {
+                    const int xn = x + dx, yn = y + dy, zn = z + dz;
+                    if (!g.inside(xn, yn, zn) || g.ground(xn, yn, zn)) return 0.0;
+                    return double(pp[g.id(xn, yn, zn)]);
+                };
+                auto lower = [&](int dx, int dy, int dz, const std::vector<float>& arr) {
+                    const int xn = x + dx, yn = y + dy, zn = z + dz;
+                    if (!g.inside(xn, yn, zn) || g.ground(xn, yn, zn)) return 0.0;
+                    const float a = arr[g.id(xn, yn, zn)];
+                    return double(ref ? char_trunc(a) : a);
+                };
+                const double Ap = double(A.w[idx]) * pp[idx] + lower(-1, 0, 0, A.x) * S(-1, 0, 0) + lower(0, -1, 0, A.y) * S(0, -1, 0) +
+                                  lower(0, 0, -1, A.z) * S(0, 0, -1) + double(A.x[idx]) * S(1, 0, 0) + double(A.y[idx]) * S(0, 1, 0) +
+                                  double(A.z[idx]) * S(0, 0, 1);
+                const double res = double(r[idx]) - Ap;
+                mx = std::max(mx, std::fabs(res));
+                l2 += res * res;
+                bmx = std::max(bmx, std::fabs(double(r[idx])));
+                bl2 += double(r[idx]) * double(r[idx]);
+            }
+    out[0] = mx; out[1] = std::sqrt(l2); out[2] = bmx; out[3] = std::sqrt(bl2);
+    return 0;
 }
 
 // the microphysics stage with the region-summed process amounts (region: lo x,y,z then hi x,y,z)

@@ -82,6 +82,7 @@ SIGNATURES = {
                                            ctypes.c_float, c_float_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "skt_reset_parameter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "skt_read_ground_height": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_size_t]),
+    "skt_read_neighbours": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t]),
     "skt_sounding_read_knmi": (ctypes.c_int, [ARCHIVE_READ_FN, ctypes.c_void_p, ctypes.POINTER(Sounding)]),
     "skt_sounding_read_dwd": (ctypes.c_int, [ctypes.c_char_p, ARCHIVE_READ_FN, ctypes.c_void_p, ctypes.POINTER(Sounding)]),
     "skt_sounding_free": (None, [ctypes.POINTER(Sounding)]),

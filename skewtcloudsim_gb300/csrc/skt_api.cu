@@ -437,11 +437,16 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     skt_status worst = SKT_OK;
     if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
     cudaEventRecord(e.ev0, e.stream);
+    int done = 0;
     for (int i = 0; i < nsteps; ++i) {
         const skt_status st = run_step(e, dt, speed);
         if (st != SKT_OK) return st;
+        ++done;
         e.ground_changed = 0;  // Game/environment.cu:554
         if (!e.last_converged) worst = SKT_NOT_CONVERGED;
+        // the step's own scalar reads (Courant counts, solver stop tests) already brought the
+        // device status to the host: a step that met a NaN or Inf ends the call
+        if (e.host_sc->status != 0) break;
     }
     cudaEventRecord(e.ev1, e.stream);
     cudaEventSynchronize(e.ev1);
@@ -451,8 +456,13 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     fetch_scalars(e);
     const int dev_status = e.host_sc->status;
     if (dev_status != 0) {
-        cudaMemset(&e.sc->status, 0, sizeof(int));
-        return fail(&e, skt_status(dev_status), "a kernel gave up waiting for its streamed data (device-side wait limit)");
+        cudaMemsetAsync(&e.sc->status, 0, sizeof(int), e.stream);
+        cudaStreamSynchronize(e.stream);
+        e.host_sc->status = 0;
+        return fail(&e, skt_status(dev_status),
+                    "step " + std::to_string(done) + " of this call met a NaN or Inf (in the wind or in a pressure-solver "
+                    "reduction: a non-finite field value or a zero-density cell); the remaining steps were not run and "
+                    "the state is not valid");
     }
     return worst;
 }
@@ -549,6 +559,11 @@ skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, c
             cudaMemcpyAsync(d, src[i], sizeof(float) * n, cudaMemcpyDeviceToDevice, e.stream);
         }
     }
+    // a failed snapshot launch is reported here, before the attribute queries below clear errors
+    {
+        const skt_status snap_st = cuda_check(e, "read_fields_async (snapshot)");
+        if (snap_st != SKT_OK) return snap_st;
+    }
     cudaEventRecord(e.ev_snap, e.stream);
     cudaStreamWaitEvent(e.copy_stream, e.ev_snap, 0);
     // pinned destinations are written by a narrow kernel through their mapped addresses (it takes a
@@ -556,9 +571,10 @@ skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, c
     for (int i = 0; i < nfields; ++i) {
         const float* s = e.snap + size_t(i) * n;
         cudaPointerAttributes at{};
-        const bool mapped = cudaPointerGetAttributes(&at, dst[i]) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer &&
+        const bool known = cudaPointerGetAttributes(&at, dst[i]) == cudaSuccess;
+        if (!known) cudaGetLastError();  // an unregistered host pointer: clear only the query's own error
+        const bool mapped = known && at.type == cudaMemoryTypeHost && at.devicePointer &&
                             (reinterpret_cast<uintptr_t>(at.devicePointer) % 16) == 0 && n % 4 == 0;
-        cudaGetLastError();
         if (mapped) {
             k_snapshot<<<kHostCopyBlocks, 256, 0, e.copy_stream>>>(reinterpret_cast<const float4*>(s), static_cast<float4*>(at.devicePointer), n / 4);
             e.launches += 1;
@@ -740,6 +756,15 @@ skt_status skt_run_stage(skt_env* env, int stage, int arg, float dt, float speed
     cudaStreamSynchronize(e.stream);
     const skt_status st = cuda_check(e, "stage");
     if (out) skt_stats(env, out);
+    if (st != SKT_OK) return st;
+    fetch_scalars(e);
+    if (e.host_sc->status != 0) {  // as skt_step: a NaN or Inf met by the wind maximum or a solver reduction
+        const int dev_status = e.host_sc->status;
+        cudaMemsetAsync(&e.sc->status, 0, sizeof(int), e.stream);
+        cudaStreamSynchronize(e.stream);
+        e.host_sc->status = 0;
+        return fail(&e, skt_status(dev_status), "the stage met a NaN or Inf (wind maximum or pressure-solver reduction)");
+    }
     return st;
 }
 

@@ -268,6 +268,45 @@ skt_status skt_reset_parameter(skt_env* env, int param) {
     return check_cuda(e, "reset_parameter");
 }
 
+namespace skt {
+// The boundary class of each neighbour one cell away, by the rule ghost() applies: a neighbour
+// outside the domain takes the class of the cell itself (ground or sky), one inside is ground
+// when y <= gh. Written as the reference's Neigh record (computeNeighbourGPU,
+// Game/kernelSky.cu:1284-1316; Game/config.h:24-38): left, right, up, down, forward, backward,
+// each {outside, type} with type 0 = SKY, 1 = GROUND.
+__global__ void k_neigh_classes(Grid g, uchar2* __restrict__ out) {
+    const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    if (i >= size_t(g.N)) return;
+    const int x = int(i % g.X), y = int((i / g.X) % g.Y), z = int(i / g.XY);
+    const int dx[6] = {-1, 1, 0, 0, 0, 0}, dy[6] = {0, 0, 1, -1, 0, 0}, dz[6] = {0, 0, 0, 0, 1, -1};
+    const bool self_ground = is_ground(g, x, y, z);
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+        const int xn = x + dx[d], yn = y + dy[d], zn = z + dz[d];
+        const bool outside = !in_dom(g, xn, yn, zn);
+        const bool ground = outside ? self_ground : is_ground(g, xn, yn, zn);
+        out[i * 6 + d] = make_uchar2(outside ? 1 : 0, ground ? 1 : 0);
+    }
+}
+}  // namespace skt
+
+skt_status skt_read_neighbours(skt_env* env, uint8_t* dst, size_t n) {
+    if (!env || !dst) return report(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
+    Env& e = env->e;
+    if (n != size_t(e.g.N)) return report(&e, SKT_INVALID_ARG, "size mismatch (n is the cell count)");
+    uchar2* tmp = nullptr;
+    if (cudaMalloc(&tmp, n * 12) != cudaSuccess) {
+        cudaGetLastError();
+        return report(&e, SKT_OUT_OF_MEMORY, "neighbour record allocation failed");
+    }
+    k_neigh_classes<<<unsigned((n + 255) / 256), 256, 0, e.stream>>>(e.g, tmp);
+    e.launches += 1;
+    cudaMemcpyAsync(dst, tmp, n * 12, cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    cudaFree(tmp);
+    return check_cuda(e, "read_neighbours");
+}
+
 skt_status skt_read_ground_height(skt_env* env, int32_t* dst, size_t n) {
     if (!env || !dst) return report(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
     Env& e = env->e;

@@ -86,6 +86,17 @@ struct Scalars {
     int edit_changed;                 // an edit changed the ground store
 };
 
+// A non-finite total of a solver reduction (a dot product or squared norm over every sky cell)
+// means a NaN or Inf reached the projection: a non-finite field value or a zero density. The
+// reduction's last block records it for skt_step, which stops stepping and reports
+// SKT_NAN_DETECTED; the solver loops stop at their next host check. The reference traps only on
+// CUDA errors (Game/environment.cu:394-403) and would carry the NaNs on.
+__device__ __forceinline__ void note_nonfinite(Scalars* sc, double tot) {
+    if (!isfinite(tot)) sc->status = SKT_NAN_DETECTED;
+}
+// the same test on one float (the wind maximum's inputs)
+__device__ __forceinline__ bool nonfinite(float v) { return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u; }
+
 // one coarse level of the multigrid preconditioner (A-form coefficients and work vectors)
 struct MgLevel {
     int X = 0, Y = 0, Z = 0;

@@ -261,6 +261,7 @@ __device__ __forceinline__ bool finish(Scalars* sc, double* partials, double sum
         tot = ts;
         mall = tm;
         sc->done_blocks = 0;
+        note_nonfinite(sc, ts);
     }
     return threadIdx.x == 0;
 }
@@ -336,9 +337,11 @@ __global__ void __launch_bounds__(RT) k_resid_ff(Grid g, const float* __restrict
         mx = fmaxf(mx, fabsf(rv));
     }
     const double bs = bsum<RT>(double(acc) - double(comp), smd);
+    __shared__ float smf[RT / 32];
+    const float bm = bmax<RT>(mx, smf);  // the block's max |r| (finish publishes thread 0's value)
     double tot;
     float mall;
-    if (finish(sc, partials, bs, mx, tot, mall)) refine_record(sc, tot, mall, refine_tol, first);
+    if (finish(sc, partials, bs, bm, tot, mall)) refine_record(sc, tot, mall, refine_tol, first);
 }
 
 // (xh, xl) += e and e = 0
@@ -544,18 +547,27 @@ __device__ __forceinline__ bool finish_sum(Scalars* sc, double* partials, double
     if (tid == 0) {
         tot = ts;
         sc->done_blocks = 0;
+        note_nonfinite(sc, ts);
     }
     return tid == 0;
 }
 
-// finish_sum with a max as well (partials[kMaxPartials + bid] holds the block maxima)
+// finish_sum with a max as well: mx is each thread's own max, reduced over the block here
+// (partials[kMaxPartials + bid] holds the block maxima)
 template <int NTH>
 __device__ __forceinline__ bool finish_sum_max(Scalars* sc, double* partials, double sum, float mx, double& tot, float& mall, int tid) {
     __shared__ bool last;
     __shared__ double sd[NTH / 32];
     __shared__ float sf[NTH / 32];
+    __shared__ float sb[NTH / 32];
     const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     const int nblk = gridDim.x * gridDim.y * gridDim.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) sb[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0)
+        for (int w = 1; w < NTH / 32; ++w) mx = fmaxf(mx, sb[w]);
     if (tid == 0) {
         partials[bid] = sum;
         partials[kMaxPartials + bid] = double(mx);
@@ -583,6 +595,7 @@ __device__ __forceinline__ bool finish_sum_max(Scalars* sc, double* partials, do
         tot = ts;
         mall = t;
         sc->done_blocks = 0;
+        note_nonfinite(sc, ts);
     }
     return tid == 0;
 }
@@ -1196,7 +1209,7 @@ void mg_solve(Env& e) {
             e.launches += 1;
         }
         fetch_scalars(e);
-        if (e.host_sc->refine_done == 1) break;
+        if (e.host_sc->refine_done == 1 || e.host_sc->status != 0) break;
         // inner MG-PCG on A e = r
         const int* conv = &e.sc->converged;
         if (fused) {
@@ -1221,7 +1234,7 @@ void mg_solve(Env& e) {
                     std::swap(s_old, s_new);
                 }
                 fetch_scalars(e);
-                if (e.host_sc->converged) break;
+                if (e.host_sc->converged || e.host_sc->status != 0) break;
             }
             { ProfScope ps(e, "mg_refine");
               k_accum_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, ecor);
@@ -1263,7 +1276,7 @@ void mg_solve(Env& e) {
                 e.launches += 4;
             }
             fetch_scalars(e);
-            if (e.host_sc->converged) break;
+            if (e.host_sc->converged || e.host_sc->status != 0) break;
         }
         { ProfScope ps(e, "mg_refine");
           k_accum_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, ecor);

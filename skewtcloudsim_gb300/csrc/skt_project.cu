@@ -341,6 +341,7 @@ __device__ __forceinline__ bool publish_n(Scalars* sc, double* partials, int bid
         tot = ts;
         mxall = tm;
         sc->done_blocks = 0;
+        note_nonfinite(sc, ts);
     }
     return tid == 0;
 }
@@ -1038,7 +1039,7 @@ void launch_project(Env& e, float dtS) {
             }
         }
         fetch_scalars(e);
-        if (e.host_sc->converged) break;
+        if (e.host_sc->converged || e.host_sc->status != 0) break;
     }
     if (vec && e.cfg.pcg_fused && e.host_sc->iters > 0) {
         // the last iteration's pressure update (no later operator launch carried it)

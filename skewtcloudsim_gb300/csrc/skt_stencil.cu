@@ -3,6 +3,8 @@
 #include "skt_internal.cuh"
 #include "../../include/skewt.h"
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 namespace skt {
 
@@ -507,10 +509,12 @@ __global__ void __launch_bounds__(256) k_maxvel(Grid g, const float* __restrict_
                                                 int reference, Scalars* __restrict__ sc) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
     float m = 0.0f;
+    bool bad = false;
     if (x < g.X && y < g.Y && !is_ground(g, x, y, z)) {
         const int c = cidx(g, x, y, z);
         const bool absv = !reference || z == 0;
         float v0 = a0[c], v1 = a1[c], v2 = a2[c];
+        bad = nonfinite(v0) | nonfinite(v1) | nonfinite(v2);
         if (absv) { v0 = fabsf(v0); v1 = fabsf(v1); v2 = fabsf(v2); }
         if (v0 > m) m = v0;
         if (v1 > m) m = v1;
@@ -522,6 +526,7 @@ __global__ void __launch_bounds__(256) k_maxvel(Grid g, const float* __restrict_
         if (t > m) m = t;
     }
     if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(&sc->maxbits, __float_as_uint(m));
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) sc->status = SKT_NAN_DETECTED;  // a NaN or Inf wind
 }
 
 // flat terrain: the same max over rows y >= 1, as float4 streams with one atomic per block
@@ -529,6 +534,7 @@ __global__ void __launch_bounds__(256) k_maxvel4(int n4, int X4, int Y, int XY4,
                                                  const float4* __restrict__ a2, int reference, Scalars* __restrict__ sc) {
     __shared__ float sm[8];
     float m = 0.0f;
+    bool bad = false;
     for (int i = blockIdx.x * 256 + threadIdx.x; i < n4; i += gridDim.x * 256) {
         if ((i / X4) % Y == 0) continue;  // the ground layer
         const bool absv = !reference || i < XY4;
@@ -536,6 +542,7 @@ __global__ void __launch_bounds__(256) k_maxvel4(int n4, int X4, int Y, int XY4,
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             float e0 = v[j].x, e1 = v[j].y, e2 = v[j].z, e3 = v[j].w;
+            bad |= nonfinite(e0) | nonfinite(e1) | nonfinite(e2) | nonfinite(e3);
             if (absv) { e0 = fabsf(e0); e1 = fabsf(e1); e2 = fabsf(e2); e3 = fabsf(e3); }
             if (e0 > m) m = e0;
             if (e1 > m) m = e1;
@@ -549,6 +556,7 @@ __global__ void __launch_bounds__(256) k_maxvel4(int n4, int X4, int Y, int XY4,
         if (t > m) m = t;
     }
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) sc->status = SKT_NAN_DETECTED;  // a NaN or Inf wind
     __syncthreads();
     if (threadIdx.x == 0) {
         float b = 0.0f;
@@ -1200,8 +1208,71 @@ constexpr unsigned kNoAllocMaxCells = 1u << 21;  // 2,097,152 cells: 8 MiB of sc
 // ground cells are never read. Calls whose work overlaps on the GPU race on it.
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocMaxCells];
 
-constexpr int kNoAllocMaxDevices = 64;
-float* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+// The array's device address, looked up once per CUDA context. A context, not a device number,
+// is the key: a host framework may make its own driver-API context current on a device, and after
+// cudaDeviceReset the device's next primary context is a new one. Contexts are told apart by
+// cuCtxGetId (unique for the life of the process), reached through the runtime's driver entry
+// points so that the library needs no link against libcuda.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+struct NoAllocSlot {
+    unsigned long long ctx_id;
+    float* ptr;
+};
+constexpr int kNoAllocMaxContexts = 64;
+std::mutex g_noalloc_mu;
+NoAllocSlot g_noalloc_slots[kNoAllocMaxContexts];
+int g_noalloc_nslots = 0;
+
+bool current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = cudaDriverEntryPointSymbolNotFound;
+        void *f1 = nullptr, *f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return false;
+        get_current = (CtxGetCurrentFn)f1;
+        get_id = (CtxGetIdFn)f2;
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
+}
+
+// The scratch array's address in the current context (looked up on the first call there).
+// Returns nullptr with the error text set when no context can be made current.
+float* noalloc_scratch_address(std::string& err) {
+    unsigned long long id = 0;
+    if (!current_context_id(&id)) {
+        // no context is current yet: the runtime makes the current device's primary context
+        // current on its first call that needs one, which the lookup below is
+        float* probe = nullptr;
+        const cudaError_t e0 = cudaGetSymbolAddress((void**)&probe, g_noalloc_scratch);
+        if (e0 != cudaSuccess || !current_context_id(&id)) {
+            err = e0 != cudaSuccess ? cudaGetErrorString(e0) : "no current CUDA context";
+            return nullptr;
+        }
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    for (int i = 0; i < g_noalloc_nslots; ++i)
+        if (g_noalloc_slots[i].ctx_id == id) return g_noalloc_slots[i].ptr;
+    float* ptr = nullptr;
+    const cudaError_t e1 = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
+    if (e1 != cudaSuccess || !ptr) {
+        err = e1 != cudaSuccess ? cudaGetErrorString(e1) : "null symbol address";
+        return nullptr;
+    }
+    // the table keeps the most recent contexts: a full table drops its oldest entry
+    if (g_noalloc_nslots == kNoAllocMaxContexts) {
+        for (int i = 1; i < kNoAllocMaxContexts; ++i) g_noalloc_slots[i - 1] = g_noalloc_slots[i];
+        --g_noalloc_nslots;
+    }
+    g_noalloc_slots[g_noalloc_nslots++] = NoAllocSlot{id, ptr};
+    return ptr;
+}
 
 __global__ void k_copy_all(const float* __restrict__ src, float* __restrict__ dst, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1226,6 +1297,10 @@ extern "C" skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, i
                          "diffuse larger grids through skt_create/skt_step");
         return SKT_INVALID_ARG;
     }
+    if (nz > 65535 || (ny + BY - 1) / BY > 65535) {  // the launch grid's y and z limits
+        set_global_error("skt_diffuse_noalloc: nz must be <= 65535 and ny <= 524280 (CUDA grid limits)");
+        return SKT_INVALID_ARG;
+    }
     if (!in_dev || !out_dev || !ground_height_dev || in_dev == out_dev) {
         set_global_error("skt_diffuse_noalloc: null or aliased input/output buffer");
         return SKT_INVALID_ARG;
@@ -1235,21 +1310,13 @@ extern "C" skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, i
         set_global_error("skt_diffuse_noalloc: this field type needs its default column (and, for theta, p/ground T/ground p)");
         return SKT_INVALID_ARG;
     }
-    // Set-up, once per device and with that device current: the address of the array. In host
-    // code its name only stands in for the device symbol, so the kernels get this pointer.
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
-        set_global_error("skt_diffuse_noalloc: no usable current CUDA device");
-        return SKT_CUDA_ERROR;
-    }
-    float* scratch = g_noalloc_ptr[dev];
+    // Set-up, once per CUDA context and with it current: the address of the array. In host code
+    // its name only stands in for the device symbol, so the kernels get this pointer.
+    std::string err_text;
+    float* scratch = noalloc_scratch_address(err_text);
     if (!scratch) {
-        const cudaError_t err = cudaGetSymbolAddress((void**)&scratch, g_noalloc_scratch);
-        if (err != cudaSuccess || !scratch) {
-            set_global_error(cudaGetErrorString(err));
-            return SKT_CUDA_ERROR;
-        }
-        g_noalloc_ptr[dev] = scratch;
+        set_global_error(("skt_diffuse_noalloc: " + err_text).c_str());
+        return SKT_CUDA_ERROR;
     }
     Grid g;
     g.X = nx; g.Y = ny; g.Z = nz; g.XY = nx * ny; g.N = int(n); g.gh = ground_height_dev; g.vox = voxel;

@@ -313,6 +313,13 @@ class Environment:
         self._check(self._L.skt_read_ground_height(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), out.size))
         return out
 
+    def read_neighbours(self) -> np.ndarray:
+        """The Neigh records of every cell (computeNeighbourGPU's layout): uint8 (n, 6, 2) of
+        (outside, type) for left, right, up, down, forward, backward; type 1 = ground."""
+        out = np.empty(self.n * 12, np.uint8)
+        self._check(self._L.skt_read_neighbours(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), self.n))
+        return out.reshape(self.n, 6, 2)
+
     # -- editing between steps (the reference's editor tools) -------------------------------
     def apply_brush(self, param, size, pos, smoothness, dt, intensity, value, direction=(1.0, 0.0, 0.0), erase=False) -> bool:
         """prepareBrushGPU: returns whether the heightfield changed."""
