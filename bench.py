@@ -175,12 +175,36 @@ def cpu_baseline(workload: str, sample_shape, steps: int = 1, threads: int = 0):
                       f"(x,y,z; z vertical) sub-box, reference semantics, FP32, {used} thread(s), {el:.1f} s"}
 
 
+CPU_SAMPLE = (128, 128, 64)  # (x, y, z), z vertical: the bounded sub-box of the CPU legs (1.05M cells)
+
+
+def cpu_thread_sweep(workload: str, sample_shape):
+    """The same sub-box step at 1, 2, 4, ... threads up to the host's cores (one step each)."""
+    import oracle
+    full = oracle.lib().oc_num_threads()
+    counts, t = [], 1
+    while t < full:
+        counts.append(t)
+        t *= 2
+    counts.append(full)
+    out = []
+    for t in counts:
+        r = cpu_baseline(workload, sample_shape, 1, threads=t)
+        out.append({"threads": r["cores"], "value": round(r["value"], 1)})
+    return out
+
+
+# Arm CPU part numbers (/proc/cpuinfo "CPU part") of the cores these boxes use
+ARM_PARTS = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1", "0xd0c": "Arm Neoverse N1", "0xd49": "Arm Neoverse N2"}
+
+
 def host_cpu():
     try:
         with open("/proc/cpuinfo") as f:
             for ln in f:
                 if ln.lower().startswith(("model name", "cpu part", "hardware")):
-                    return ln.split(":", 1)[1].strip()
+                    v = ln.split(":", 1)[1].strip()
+                    return f"{ARM_PARTS[v]} (CPU part {v})" if v in ARM_PARTS else v
     except Exception:
         pass
     return None
@@ -189,7 +213,7 @@ def host_cpu():
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    sample = (128, 128, 64)
+    sample = CPU_SAMPLE
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, sample, 1)
@@ -206,6 +230,11 @@ def run_reference(args, rank, world):
            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": r["cores"], "kind": "port",
                             "sample": r["sample"]},
            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    # one whole workload the CPU finishes in seconds: the plain-64x64x32 configuration at its full size
+    c1 = cpu_baseline("plain-64x64x32", (64, 64, 32), 1)
+    out["full_size_run"] = {"workload": "plain-64x64x32", "value": c1["value"], "unit": "cell-steps/s",
+                            "cores": c1["cores"], "same_config": True, "sample": c1["sample"]}
+    out["host"] = {"nproc": os.cpu_count(), "cpu": host_cpu()}
     print(json.dumps(out), flush=True)
 
 
@@ -221,11 +250,33 @@ def step_bytes(mode, pcg_iters, outer):
     return 2534.0 + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
 
 
+# plain_textbook: the plain Jacobi-PCG on the textbook (symmetric) operator the mixed mode solves,
+# run to the reference's own stop test (max |r| <= 1e-5) without the 200-iteration cap
+TEXTBOOK_MAX_ITER = 20000
+
+
+def mode_config(args, mode):
+    from skewtcloudsim_gb300 import SolverConfig
+    if mode == "plain":
+        return SolverConfig(semantics=args.semantics, precision=0, mg_half=args.mg_half, pcg_fused=args.pcg_fused)
+    if mode == "plain_textbook":
+        return SolverConfig(semantics=1, precision=0, pcg_max_iter=TEXTBOOK_MAX_ITER, pcg_fused=args.pcg_fused)
+    return SolverConfig(semantics=1, precision=1, mg_half=args.mg_half, pcg_fused=args.pcg_fused)
+
+
+def survey_step_bytes(mode, pcg_iters, outer):
+    """The scope table's algorithmic model of a cell-step: 2558 B of stages plus 52 B per Jacobi-PCG
+    iteration (matrix-free: the operator's coefficients formed from the density, 4 B, instead of
+    four stored coefficient arrays, 16 B) plus 40 B per refinement step. The library streams the
+    stored coefficients (60 B per plain iteration, 1.15x the model's 52 B)."""
+    assert mode != "mixed"  # the model has no term for the V-cycle
+    return 2558.0 + 52.0 * pcg_iters
+
+
 def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
-    from skewtcloudsim_gb300 import Environment, SolverConfig
-    sem = args.semantics if mode == "plain" else 1
-    cfg = SolverConfig(semantics=sem, precision=1 if mode == "mixed" else 0, mg_half=args.mg_half,
-                       pcg_fused=args.pcg_fused)
+    from skewtcloudsim_gb300 import Environment
+    cfg = mode_config(args, mode)
+    sem = cfg.semantics
     env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
     env.init_from(init)
     for _ in range(args.warmup):
@@ -261,7 +312,8 @@ def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
     env.close()
     return {"mode": mode, "semantics": "reference" if sem == 0 else "textbook", "value": value, "ms_per_step": ms_per_step,
             "launches": int(launches), "clocks": clk.summary(), "prof": prof, "pcg_iters": sd["pcg_iters"],
-            "outer": sd.get("outer_iters", 0), "converged": sd["converged"], "residual": sd["pcg_residual"]}
+            "outer": sd.get("outer_iters", 0), "converged": sd["converged"], "residual": sd["pcg_residual"],
+            "pcg_max_iter": cfg.pcg_max_iter}
 
 
 def run_ensemble(args, rank, world, local, pg, torch):
@@ -327,8 +379,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="precision-512x512x256")
-    ap.add_argument("--mode", default="both", choices=["plain", "mixed", "both"],
-                    help="both: plain (reference semantics, the headline) and mixed (reported beside it)")
+    ap.add_argument("--mode", default="both", choices=["plain", "mixed", "plain_textbook", "both"],
+                    help="both: plain (reference semantics, the headline), mixed and plain_textbook (reported beside it)")
     ap.add_argument("--semantics", type=int, default=0)
     ap.add_argument("--mg-half", type=int, default=1, help="mixed: FP16 finest-level coefficients in the V-cycle")
     ap.add_argument("--pcg-fused", type=int, default=1,
@@ -356,7 +408,7 @@ def main():
     shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
     init, dt, speed = sounding.workload(args.workload, scale=shape)
     cells = init.nx * init.ny * init.nz
-    modes = ["plain", "mixed"] if args.mode == "both" else [args.mode]
+    modes = ["plain", "mixed", "plain_textbook"] if args.mode == "both" else [args.mode]
     res = {m: run_mode(args, m, init, dt, speed, cells, world, local, pg, torch) for m in modes}
     head = res[modes[0]]
     prof = head["prof"]
@@ -380,7 +432,15 @@ def main():
     step_ms_prof = sum(v["ms"] for v in prof.values())
     bstep = step_bytes(head["mode"], head["pcg_iters"], head["outer"])
     step_model = {"bytes_per_cell_step": bstep, "achieved_gbs": round(bstep * head["value"] / 1e9, 1),
-                  "frac": round(bstep * head["value"] / 1e9 / peak, 4), "peak_source": peak_kind}
+                  "frac": round(bstep * head["value"] / 1e9 / peak, 4), "peak_source": peak_kind,
+                  "model": "the library's own bytes: 2534 B of stages + 60 B per plain PCG iteration (stored coefficients)"}
+    if head["mode"] != "mixed":
+        sb = survey_step_bytes(head["mode"], head["pcg_iters"], head["outer"])
+        step_model["scope_model"] = {
+            "bytes_per_cell_step": sb, "frac": round(sb * head["value"] / 1e9 / peak, 4),
+            "model": "2558 B of stages + 52 B per matrix-free Jacobi-PCG iteration; the library streams four stored "
+                     "coefficient arrays (16 B) where the model reads the density (4 B): 60 / 52 = 1.15x the "
+                     "model's solver bytes"}
 
     # ---- end to end through the C ABI from host buffers (headline mode) -------------------
     e2e = None
@@ -416,9 +476,8 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        cpu = cpu_baseline(args.workload, (128, 128, 64), 1)
-        one = cpu_baseline(args.workload, (64, 64, 32), 1, threads=1)
-        cpu["single_thread"] = {"value": one["value"], "sample": one["sample"]}
+        cpu = cpu_baseline(args.workload, CPU_SAMPLE, 1)
+        cpu["thread_sweep"] = cpu_thread_sweep(args.workload, CPU_SAMPLE)
         cpu["host"] = {"nproc": os.cpu_count(), "cpu": host_cpu()}
 
     field_mb = cells * 4 / 1e6
@@ -434,6 +493,22 @@ def main():
            "roofline": roofline, "step_roofline": step_model, "cpu_baseline": cpu, "e2e": e2e,
            "gpu_launches": head["launches"], "clocks": head["clocks"],
            "profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "profile_step_ms": round(step_ms_prof, 3)}
+    if head["mode"] == "plain" and head["semantics"] == "reference":
+        out["config"]["pcg_note"] = (f"reference semantics: the PCG stops at its {head['pcg_max_iter']}-iteration cap "
+                                     f"without converging (converged={head['converged']}, max residual "
+                                     f"{head['residual']:.3g} > 1e-5), as the reference's does")
+    if "plain_textbook" in res:
+        t = res["plain_textbook"]
+        out["plain_textbook"] = {
+            "value": t["value"], "ms_per_step": t["ms_per_step"], "semantics": "textbook",
+            "pcg_iters_per_step": t["pcg_iters"], "converged": t["converged"], "max_residual": t["residual"],
+            "pcg_max_iter": t["pcg_max_iter"], "gpu_launches": t["launches"], "clocks": t["clocks"],
+            "note": "the plain Jacobi-PCG on the textbook (symmetric) operator the mixed mode solves, run without the "
+                    "iteration cap to the reference's stop test max |r| <= 1e-5",
+            "step_roofline": {"bytes_per_cell_step": step_bytes("plain", t["pcg_iters"], 0),
+                              "frac": round(step_bytes("plain", t["pcg_iters"], 0) * t["value"] / 1e9 / peak, 4),
+                              "scope_model_frac": round(survey_step_bytes("plain", t["pcg_iters"], 0) * t["value"] / 1e9 / peak, 4)},
+            "profile_ms": {k: round(v["ms"], 3) for k, v in t["prof"].items()}}
     if "mixed" in res and head["mode"] != "mixed":
         m = res["mixed"]
         out["mixed"] = {"value": m["value"], "ms_per_step": m["ms_per_step"], "speedup_vs_plain": round(m["value"] / head["value"], 3),
@@ -442,6 +517,11 @@ def main():
                         "step_roofline": {"bytes_per_cell_step": step_bytes("mixed", m["pcg_iters"], m["outer"]),
                                           "frac": round(step_bytes("mixed", m["pcg_iters"], m["outer"]) * m["value"] / 1e9 / peak, 4)},
                         "clocks": m["clocks"], "profile_ms": {k: round(v["ms"], 3) for k, v in m["prof"].items()}}
+        if "plain_textbook" in res:
+            out["mixed"]["speedup_vs_plain_textbook"] = round(m["value"] / res["plain_textbook"]["value"], 3)
+        out["mixed"]["note"] = ("speedup_vs_plain: against the capped reference-semantics PCG (the drop-in headline, "
+                                "not converged); speedup_vs_plain_textbook: against the plain Jacobi-PCG on the same "
+                                "textbook operator run to convergence")
     if rank == 0:
         print(json.dumps(out), flush=True)
     if pg:

@@ -172,7 +172,49 @@ def build_readtable(force: bool = False):
     return outs
 
 
+def colors_path():
+    return os.path.join(OUT, "libref_colors.so")
+
+
+def _setcolors_body():
+    """The statements of editor::setColors (Game/editor.cpp:53-112), copied at build time."""
+    with open(os.path.join(REF, "Game", "editor.cpp"), encoding="utf-8", errors="replace") as f:
+        lines = f.read().splitlines()
+    start = next(i for i, ln in enumerate(lines) if ln.strip() == "void editor::setColors()")
+    if lines[start + 1].strip() != "{":
+        raise RuntimeError("unexpected Game/editor.cpp layout")
+    end = next(i for i in range(start + 2, len(lines)) if lines[i].rstrip() == "}")
+    p = os.path.join(OUT, "setcolors_body.inc")
+    with open(p, "w") as f:
+        f.write("\n".join(lines[start + 2:end]) + "\n")
+    return p
+
+
+def build_colors(force: bool = False):
+    """The reference's colour schemes: editor::setColors' statements and
+    Engine/source/rendering/colors.cpp, unmodified, with oracle/ref_colors.cpp (g++, host code)."""
+    src = os.path.join(REF, "Engine", "source", "rendering", "colors.cpp")
+    if not os.path.exists(src) or not os.path.exists(os.path.join(REF, "Game", "editor.cpp")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    so = colors_path()
+    harness = os.path.join(HERE, "ref_colors.cpp")
+    if os.path.exists(so) and not force and os.path.getmtime(so) >= os.path.getmtime(harness):
+        return so
+    _setcolors_body()
+    inc = ["-I", os.path.join(HERE, "colors_stubs"), "-I", OUT, "-I", os.path.join(REF, "Engine", "include"),
+           "-I", os.path.join(REF, "Engine", "external")]
+    force_inc = ["-include", os.path.join(HERE, "colors_stubs", "std_headers.hpp")]
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", *force_inc, *inc, harness, src,
+                        "-o", so + ".tmp"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference colour schemes build failed:\n{r.stderr[-4000:]}")
+    os.replace(so + ".tmp", so)
+    return so
+
+
 if __name__ == "__main__":
     print(build_cubins(force=True))
     print(build_harness(force=True))
     print(build_readtable(force=True))
+    print(build_colors(force=True))

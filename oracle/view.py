@@ -5,8 +5,11 @@ editor::setColors (Game/editor.cpp:53-112) evaluated as bee::colorScheme::getCol
 cell-centred wind of environment::getUV (Game/environment.cpp:2083-2095). Float32 arithmetic
 operation by operation (numpy float32 arrays, no fused multiply-add).
 
-Parity unpinned against the reference itself (its view only draws through OpenGL); the tests
-pin the colour-scheme evaluation with hand-computed known answers.
+The colour-scheme evaluation is pinned to the reference itself: tests/test_cpu_volume.py compares
+get_color bit for bit with the reference's own getColor and setColors, compiled from the reference
+sources (oracle/build_ref.py build_colors, oracle/ref_colors.cpp). The per-voxel choices of
+viewSky/viewGround (which field feeds which scheme, the hidden and ground voxels) are restated from
+the source: the reference evaluates them only while drawing through OpenGL.
 """
 import numpy as np
 

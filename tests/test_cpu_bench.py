@@ -18,6 +18,8 @@ def test_reference_arm_prints_the_contract_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and "sub-box" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    full = d["full_size_run"]
+    assert full["workload"] == "plain-64x64x32" and full["same_config"] is True and full["value"] > 0
 
 
 def test_step_byte_model():
@@ -26,3 +28,5 @@ def test_step_byte_model():
     assert bench.step_bytes("plain", 200, 0) == 2534.0 + 60.0 * 200
     assert bench.STAGE_BYTES["pcg_matvec"] + bench.STAGE_BYTES["pcg_update"] == 60.0
     assert 40.0 < bench.MEASURED_TRAFFIC_PER_CELL["pcg_matvec"] < 41.0
+    # the scope table's model of the same step: 2558 B of stages + 52 B per matrix-free iteration
+    assert bench.survey_step_bytes("plain", 200, 0) == 2558.0 + 52.0 * 200

@@ -1,8 +1,13 @@
 """Headless view and volume export on the CPU: the oracle's colour-scheme evaluation against
-hand-computed known answers of bee::colorScheme::getColor (Engine/source/rendering/colors.cpp:28-67)
-with the schemes of editor::setColors (Game/editor.cpp:53-112), the voxel kinds of viewSky /
-viewGround on a grid with terrain and a slice, and the brick, VTK and checkpoint file formats
-(round trips; the GPU side is tests/test_gpu_volume.py)."""
+the reference's own bee::colorScheme::getColor (Engine/source/rendering/colors.cpp:28-67) filled by
+its own editor::setColors (Game/editor.cpp:53-112), both compiled here from the reference sources
+(oracle/build_ref.py build_colors; the test is skipped where the reference checkout is absent),
+and against hand-computed known answers; the voxel kinds of viewSky / viewGround on a grid with
+terrain and a slice, and the brick, VTK and checkpoint file formats (round trips; the GPU side is
+tests/test_gpu_volume.py)."""
+import ctypes
+import os
+
 import numpy as np
 import pytest
 
@@ -10,6 +15,46 @@ from oracle import view as ov
 from skewtcloudsim_gb300 import volume
 
 f32 = np.float32
+
+
+def _reference_colors():
+    from oracle import build_ref
+    so = build_ref.colors_path()
+    if not os.path.exists(so):
+        try:
+            so = build_ref.build_colors()
+        except Exception as exc:  # a build failure is a failure, not a skip
+            pytest.fail(f"reference colour schemes did not build: {exc}")
+    if not so or not os.path.exists(so):
+        pytest.skip("the reference checkout is not available to build its colour schemes")
+    L = ctypes.CDLL(so)
+    L.rc_get_color.argtypes = [ctypes.c_char_p, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
+    L.rc_get_color.restype = ctypes.c_int
+    return L
+
+
+@pytest.mark.parametrize("name", sorted(ov.SCHEMES))
+def test_schemes_match_the_reference_getcolor(name):
+    """Every colour the view can give, bit for bit: each key, its float neighbours on both sides,
+    a dense sweep through and beyond the scheme's range, random values, and NaN/Inf."""
+    L = _reference_colors()
+    keys = ov.SCHEMES[name][0].astype(np.float32)
+    lo, hi = float(keys.min()), float(keys.max())
+    span = hi - lo
+    rng = np.random.default_rng(11)
+    vals = np.concatenate([keys, np.nextafter(keys, np.float32(np.inf)), np.nextafter(keys, np.float32(-np.inf)),
+                           np.linspace(lo - 0.1 * span, hi + 0.1 * span, 4001, dtype=np.float32),
+                           rng.uniform(lo, hi, 4000).astype(np.float32),
+                           np.geomspace(1e-6, max(hi, 1e-3), 500).astype(np.float32),
+                           np.float32([np.nan, np.inf, -np.inf, 0.0, -0.0])]).astype(np.float32)
+    want = np.empty((vals.size, 3), np.float32)
+    buf = (ctypes.c_float * 3)()
+    for i, v in enumerate(vals):
+        assert L.rc_get_color(name.encode(), ctypes.c_float(v), buf) >= 0
+        want[i] = buf[:]
+    got = ov.get_color(name, vals)
+    bad = np.nonzero((got.view(np.uint32) != want.view(np.uint32)).any(axis=1))[0]
+    assert bad.size == 0, [(float(vals[i]), got[i].tolist(), want[i].tolist()) for i in bad[:5]]
 
 
 def test_scheme_known_answers():
