@@ -34,7 +34,7 @@ typedef enum {
     SKT_CUDA_ERROR = 2,
     SKT_NOT_CONVERGED = 3, /* the PCG hit its iteration cap; the step still completed */
     SKT_NAN_DETECTED = 4,  /* a step met a NaN or Inf (wind maximum or pressure-solver reduction); stepping stopped */
-    SKT_TIMEOUT = 5,       /* reserved, never returned: no kernel here waits on another */
+    SKT_TIMEOUT = 5,       /* a kernel's bounded wait for its own streamed data (TMA copies) ran out */
     SKT_OUT_OF_MEMORY = 6,
     SKT_NOT_INITIALIZED = 7,
     SKT_COURANT_LIMIT = 8  /* reserved, never returned: a step runs any substep count up to max_substeps */
@@ -215,6 +215,46 @@ skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, int field_ty
                                const float* in_dev, float* out_dev, const int32_t* ground_height_dev,
                                const float* default_column_dev, const float* p_dev, const float* ground_T_dev,
                                const float* ground_p_dev, void* stream);
+
+/* ---- Launch-shape tuning (no counterpart in the reference: its launch shapes are fixed) ---- */
+
+/* Launch shapes of the stencil kernels. None of them changes the results (every cell is computed
+ * with the same arithmetic from the same neighbour values); they change only the speed.
+ * diffuse_depth: sweeps per diffusion pass, 1 or 2 (temporal blocking: two Jacobi sweeps per trip
+ * through HBM, input planes streamed by TMA, flat terrain); diffuse_rows: rows per warp of the
+ * two-sweep kernel's tile, 4 or 8 (the intermediate sweep is recomputed on the tile's edge rows);
+ * *_bps: blocks per SM in the grid of the diffusion (one-sweep and two-sweep) and PPM (x, y, z
+ * pass) marches, which sets their run lengths. from_cache and the times are outputs of
+ * skt_autotune. */
+typedef struct {
+    int diffuse_depth;
+    int diffuse_rows;
+    int diffuse_bps;
+    int diffuse2_bps;
+    int ppm_x_bps;
+    int ppm_y_bps;
+    int ppm_z_bps;
+    int from_cache;   /* skt_autotune: 1 when the shapes came from the cache file */
+    float diffuse_ms; /* skt_autotune: one diffusion (all sweeps) with the chosen shapes */
+    float advect_ms;  /* skt_autotune: one advection (all passes and substeps) with the chosen shapes */
+} skt_tuning;
+
+#define SKT_TUNE_FORCE 1 /* skt_autotune: measure even when the cache has an entry */
+
+/* The environment's current launch shapes. */
+skt_status skt_get_tuning(skt_env* env, skt_tuning* out);
+
+/* Sets the launch shapes (the output fields are ignored). SKT_INVALID_ARG for values out of range. */
+skt_status skt_set_tuning(skt_env* env, const skt_tuning* t);
+
+/* Chooses the launch shapes for this grid on this GPU: with cache_path set and an entry for the GPU
+ * name and grid in that file (and no SKT_TUNE_FORCE), the entry is applied; otherwise every
+ * candidate shape is timed on scratch copies of the environment's own fields (a few hundred
+ * milliseconds at 512x256x512), candidates whose results differ from the default shapes' in any
+ * bit are rejected, the fastest are applied and, with cache_path set, written to the cache (a JSON
+ * object, one entry per line). Call between steps; the fields are not changed. Allocates one small
+ * device counter while measuring. */
+skt_status skt_autotune(skt_env* env, const char* cache_path, int flags, skt_tuning* out);
 
 /* ---- Diagnostics (the reference's data graph and debug views) ---------------------------- */
 

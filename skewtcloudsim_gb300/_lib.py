@@ -98,6 +98,19 @@ SIGNATURES = {
     "skt_version": (ctypes.c_char_p, []),
 }
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("diffuse_depth", ctypes.c_int), ("diffuse_rows", ctypes.c_int), ("diffuse_bps", ctypes.c_int),
+                ("diffuse2_bps", ctypes.c_int), ("ppm_x_bps", ctypes.c_int), ("ppm_y_bps", ctypes.c_int),
+                ("ppm_z_bps", ctypes.c_int), ("from_cache", ctypes.c_int), ("diffuse_ms", ctypes.c_float),
+                ("advect_ms", ctypes.c_float)]
+
+
+SIGNATURES.update({
+    "skt_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "skt_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "skt_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(Tuning)]),
+})
+
 _lib = None
 
 

@@ -20,7 +20,7 @@ DRIVER = os.path.join(BUILD, "skt_run")
 ROOT = os.path.dirname(HERE)
 
 SOURCES = ["skt_api.cu", "skt_stencil.cu", "skt_project.cu", "skt_micro.cu", "skt_mg.cu", "skt_edit.cu",
-           "skt_sounding.cu", "skt_export.cu"]
+           "skt_sounding.cu", "skt_export.cu", "skt_tune.cu"]
 # host arithmetic that must round like the reference's (no fused multiply-add contraction)
 PER_SOURCE = {"skt_sounding.cu": ["-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -122,9 +122,22 @@ struct SolverCfg {
     int pcg_fused;       // plain: search step and pressure update fused into the operator
 };
 
+// Launch shapes of the kernels whose best shape depends on the grid and the GPU, chosen by
+// skt_autotune (skt_tune.cu) and otherwise these defaults (hand-measured at 512x256x512).
+struct Tuning {
+    int diffuse_depth = 1;   // sweeps per diffusion pass: 1, or 2 (temporal blocking, k_diffuse2)
+    int diffuse_h = 8;       // k_diffuse2: rows per warp (4 or 8)
+    int diffuse_bps = 32;    // k_diffuse4: blocks per SM in the grid (z-run length)
+    int diffuse2_bps = 8;    // k_diffuse2: blocks per SM in the grid (z-run length)
+    int ppm_bps = 16;        // k_ppm4x: blocks per SM (z-run length)
+    int ppmz_bps = 8;        // k_ppm4z: blocks per SM (z-run length)
+    int ppmy_bps = 32;       // k_ppm4y: blocks per SM (y-run length)
+};
+
 struct Env {
     Grid g{};
     SolverCfg cfg{};
+    Tuning tune{};
     int device = 0;
     cudaStream_t stream = nullptr;
     void* pool = nullptr;

@@ -2,6 +2,7 @@
 // buoyancy and the equation of state.
 #include "skt_internal.cuh"
 #include "../../include/skewt.h"
+#include <cuda.h>
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -18,6 +19,14 @@ inline dim3 cell_grid(const Grid& g) { return dim3((g.X + BX - 1) / BX, (g.Y + B
 // (Game/kernelSky.cu:95-100)
 __device__ __forceinline__ float theta_ground(const float* p, const float* Tg, const float* Pg, int idx, int idxg) {
     return potentialTemp(Tg[idxg] - 273.15f, p[idx], Pg[idxg]) + 273.15f;
+}
+
+// One cell of a Jacobi sweep, (c + k (l + r + u + d + f + b)) / (1 + 6k) with the division as a
+// multiplication by rinv = 1 / (1 + 6k) (diffuseRedBlack Game/kernelSky.cu:110): the sum in this
+// order and the fused multiply-add spelt out, so that every kernel that sweeps gives the same bits.
+__device__ __forceinline__ float jacobi(float c, float l, float r, float u, float d, float f, float b, float k, float rinv) {
+    const float s = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(l, r), u), d), f), b);
+    return __fmul_rn(__fmaf_rn(k, s, c), rinv);
 }
 
 // One Jacobi sweep of the colour-split diffusion (diffuseRedBlack Game/kernelSky.cu:43-115; both
@@ -59,7 +68,7 @@ __global__ void __launch_bounds__(256) k_diffuse(Grid g, const float* __restrict
             }
         }
     }
-    out[c] = (in[c] + k * (l + r + u + d + f + b)) * (1.0f / (1 + 6 * k));
+    out[c] = jacobi(in[c], l, r, u, d, f, b, k, 1.0f / (1 + 6 * k));
 }
 
 // Vectorised sweep for flat terrain (ground = the y = 0 layer) and X % 4 == 0: four cells per
@@ -120,14 +129,263 @@ __global__ void __launch_bounds__(32 * DVY) k_diffuse4(Grid g, int zlen, const f
             if (lane == 31 || x0 + 4 >= X) qr = (x0 + 4 < X) ? in[c + 4] : side_val(sides, qc.w, dy);
             if (THETA && y == 1) qd = ld4f(face, x0 + z * X);  // theta's ground face (diffuseRedBlack :97)
             float4 o;
-            o.x = (qc.x + k * (ql + qc.y + qu.x + qd.x + qf.x + qb.x)) * rinv;
-            o.y = (qc.y + k * (qc.x + qc.z + qu.y + qd.y + qf.y + qb.y)) * rinv;
-            o.z = (qc.z + k * (qc.y + qc.w + qu.z + qd.z + qf.z + qb.z)) * rinv;
-            o.w = (qc.w + k * (qc.z + qr + qu.w + qd.w + qf.w + qb.w)) * rinv;
+            o.x = jacobi(qc.x, ql, qc.y, qu.x, qd.x, qf.x, qb.x, k, rinv);
+            o.y = jacobi(qc.y, qc.x, qc.z, qu.y, qd.y, qf.y, qb.y, k, rinv);
+            o.z = jacobi(qc.z, qc.y, qc.w, qu.z, qd.z, qf.z, qb.z, k, rinv);
+            o.w = jacobi(qc.w, qc.z, qr, qu.w, qd.w, qf.w, qb.w, k, rinv);
             *reinterpret_cast<float4*>(out + c) = o;
         }
         qb = qc;
         qc = qf;
+    }
+}
+
+// Two Jacobi sweeps in one pass (temporal blocking of depth 2), flat terrain, X % 4 == 0.
+//
+// Tiles: a block of D2WARPS warps covers 28 x cells and D2WARPS*H rows and marches a run of z
+// planes. The input planes stream through a ring of D2SLOTS shared-memory slots, each filled by one
+// TMA copy (cp.async.bulk.tensor) of a 36 x (D2WARPS*H + 4) box: the tile with a halo of 2 cells on
+// every side (4 on the left, so that the copy starts on a 16-byte boundary), issued D2SLOTS planes
+// ahead by one thread and completed on an mbarrier. The copies in flight, not the registers, hide
+// the memory latency. Each thread owns one x cell (lanes 2..29 write; lanes 0, 1, 30, 31 are the
+// x halo of the intermediate sweep) and H rows: it keeps three planes of the input (rows y0-2 ..
+// y0+H+1) and three planes of the intermediate sweep (rows y0-1 .. y0+H) in registers, recomputing
+// the intermediate rows next to the neighbouring warps instead of exchanging them. Every cell of
+// either sweep is computed with jacobi() from the same neighbour values as k_diffuse4, ghost values
+// of each sweep included, so the pass equals two single sweeps bit for bit, while the field makes
+// one trip through HBM per two sweeps instead of two.
+constexpr int D2OUT = 28;   // cells a warp writes along x
+constexpr int D2WARPS = 8;  // warps per block, stacked in y
+constexpr int D2BW = D2OUT + 8;  // box width: 36 floats = 144 bytes
+constexpr int D2SLOTS = 6;  // ring depth (planes in flight per block)
+constexpr unsigned kMbarSpinLimit = 1u << 20;  // try_wait rounds before a wait is declared stuck
+
+template <int H>
+struct D2Rows {
+    float v[H + 4];  // input rows y0-2 .. y0+H+1 (the intermediate sweep uses the first H+2)
+};
+template <int H>
+constexpr int d2_box_rows() { return H * D2WARPS + 4; }
+template <int H>
+constexpr int d2_slot_bytes() { return ((D2BW * d2_box_rows<H>() * 4 + 127) / 128) * 128; }
+template <int H>
+constexpr int d2_smem_bytes() { return D2SLOTS * d2_slot_bytes<H>() + D2SLOTS * 8; }
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// a bounded wait: false when the phase did not complete within kMbarSpinLimit rounds
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (unsigned i = 0; i < kMbarSpinLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <bool THETA, int H>
+__global__ void __launch_bounds__(32 * D2WARPS) k_diffuse2(const __grid_constant__ CUtensorMap tin, Grid g, int zlen,
+                                                          float* __restrict__ out, int sides, int ground, const float* __restrict__ def,
+                                                          float k, const float* __restrict__ face, Scalars* __restrict__ sc) {
+    extern __shared__ __align__(128) unsigned char d2_smem[];
+    constexpr int BR = d2_box_rows<H>();
+    constexpr int SLOT = d2_slot_bytes<H>();
+    constexpr unsigned BOX_BYTES = D2BW * BR * 4;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(d2_smem + D2SLOTS * SLOT);
+    const int lane = threadIdx.x, wy = threadIdx.y;
+    const int tid = lane + 32 * wy;
+    const int bx0 = int(blockIdx.x) * D2OUT - 4;  // box origin: a multiple of 4 cells (16 bytes)
+    const int by0 = 1 + int(blockIdx.y) * H * D2WARPS - 2;
+    const int x = bx0 + 2 + lane;
+    const int y0 = 1 + (int(blockIdx.y) * D2WARPS + wy) * H;  // the warp's first written row
+    const int zs = blockIdx.z * zlen, ze = min(zs + zlen, g.Z);
+    const int X = g.X, Y = g.Y, Z = g.Z, XY = g.XY;
+    const int zlo = max(zs - 2, 0), nplanes = min(ze + 1, Z - 1) - zlo + 1;
+    const bool xin = x >= 0 && x < X;
+    const int xc = min(max(x, 0), X - 1);
+    const int srcl = lane - (x - xc);  // the lane holding the clamped (boundary) cell
+    const bool xedge = blockIdx.x == 0 || bx0 + 2 + 31 >= X;  // block-uniform
+    const bool top = y0 + H + 1 >= Y;                        // warp-uniform
+    const float rinv = 1.0f / (1 + 6 * k);
+    const float gv = ground == DIRICHLET ? 0.0f : (def ? def[0] : 0.0f);
+    const float dtop = def ? def[Y - 1] : 0.0f;
+    auto dval = [&](int y) { return def ? __ldg(def + y) : 0.0f; };
+    // the value below the first sky row: the ground ghost, or theta's ground face of the plane
+    auto down = [&](int z) { return THETA ? __ldg(face + xc + z * X) : gv; };
+
+    if (tid == 0) {
+        for (int s = 0; s < D2SLOTS; ++s) mbar_init(&bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int issued = 0;  // producer (thread 0): planes whose copy has been issued
+    auto issue = [&](int q) {
+        const int slot = q % D2SLOTS;
+        mbar_expect_tx(&bar[slot], BOX_BYTES);
+        tma_load_3d(d2_smem + slot * SLOT, &tin, &bar[slot], bx0, by0, zlo + q);
+    };
+    if (tid == 0) {
+        for (; issued < min(D2SLOTS, nplanes); ++issued) issue(issued);
+    }
+    bool stuck = false;
+    // Input plane z (planes are consumed in increasing order) into r: the slot's rows of this
+    // thread, then the ghost rows and lanes. Rows <= 0 take the value below the first sky row,
+    // rows >= Y the side ghost of row Y-1, lanes outside the grid the side ghost of the boundary lane.
+    auto load_plane = [&](D2Rows<H>& r, int z) {
+        const int q = z - zlo, slot = q % D2SLOTS;
+        const bool ok = mbar_wait(&bar[slot], unsigned(q / D2SLOTS) & 1u);
+        const float* sm = reinterpret_cast<const float*>(d2_smem + slot * SLOT) + wy * H * D2BW + lane + 2;
+#pragma unroll
+        for (int i = 0; i < H + 4; ++i) {
+            const int y = y0 - 2 + i;
+            r.v[i] = (ok && y >= 1 && y < Y && xin) ? sm[i * D2BW] : 0.0f;
+        }
+        // every thread has read the slot: it can be refilled (a stuck copy stops the whole block)
+        if (__syncthreads_or(!ok)) {
+            stuck = true;
+            return;
+        }
+        if (tid == 0 && issued < nplanes) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(issued++);
+        }
+        if (y0 == 1) {
+            const float dv = down(z);
+            r.v[0] = dv;
+            r.v[1] = dv;
+        }
+        if (top) {
+            float t = 0.0f;  // row Y-1, picked with constant indices so that r stays in registers
+#pragma unroll
+            for (int i = 0; i < H + 4; ++i)
+                if (y0 - 2 + i == Y - 1) t = r.v[i];
+            const float gt = side_val(sides, t, dtop);
+#pragma unroll
+            for (int i = 0; i < H + 4; ++i)
+                if (y0 - 2 + i >= Y) r.v[i] = gt;
+        }
+        if (xedge) {
+#pragma unroll
+            for (int i = 0; i < H + 4; ++i) {
+                const float b = __shfl_sync(0xffffffffu, r.v[i], srcl);
+                const int y = y0 - 2 + i;
+                if (!xin && y >= 1 && y < Y) r.v[i] = side_val(sides, b, dval(y));
+            }
+        }
+    };
+    // the side ghost of a whole plane (z = -1 or z = Z) from the boundary plane b
+    auto ghost_plane = [&](D2Rows<H>& r, const D2Rows<H>& b, int nrows, int ylo) {
+#pragma unroll
+        for (int i = 0; i < H + 4; ++i) {
+            if (i >= nrows) break;
+            const int y = ylo + i;
+            r.v[i] = (y >= 1 && y < Y) ? side_val(sides, b.v[i], dval(y)) : b.v[i];
+        }
+    };
+    // Intermediate sweep of plane z into m (rows y0-1 .. y0+H) from input planes a (z-1), b (z),
+    // c (z+1); then its ghost rows and lanes.
+    auto sweep1 = [&](D2Rows<H>& m, const D2Rows<H>& a, const D2Rows<H>& b, const D2Rows<H>& c, int z) {
+#pragma unroll
+        for (int j = 0; j < H + 2; ++j) {
+            const float ctr = b.v[j + 1];
+            const float l = __shfl_up_sync(0xffffffffu, ctr, 1), r = __shfl_down_sync(0xffffffffu, ctr, 1);
+            m.v[j] = jacobi(ctr, l, r, b.v[j + 2], b.v[j], c.v[j + 1], a.v[j + 1], k, rinv);
+        }
+        if (y0 == 1) m.v[0] = down(z);  // row 0: ground, not swept
+        if (top) {
+            float t = 0.0f;
+#pragma unroll
+            for (int j = 0; j < H + 2; ++j)
+                if (y0 - 1 + j == Y - 1) t = m.v[j];
+            const float gt = side_val(sides, t, dtop);
+#pragma unroll
+            for (int j = 0; j < H + 2; ++j)
+                if (y0 - 1 + j >= Y) m.v[j] = gt;
+        }
+        if (xedge) {
+#pragma unroll
+            for (int j = 0; j < H + 2; ++j) {
+                const float bnd = __shfl_sync(0xffffffffu, m.v[j], srcl);
+                const int y = y0 - 1 + j;
+                if (!xin && y >= 1 && y < Y) m.v[j] = side_val(sides, bnd, dval(y));
+            }
+        }
+    };
+    // Second sweep of plane z from intermediate planes a (z-1), b (z), c (z+1): rows y0 .. y0+H-1.
+    auto sweep2 = [&](const D2Rows<H>& a, const D2Rows<H>& b, const D2Rows<H>& c, int z) {
+        const bool wr = xin && lane >= 2 && lane < 2 + D2OUT;
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+            const float ctr = b.v[j + 1];
+            const float l = __shfl_up_sync(0xffffffffu, ctr, 1), r = __shfl_down_sync(0xffffffffu, ctr, 1);
+            const float o = jacobi(ctr, l, r, b.v[j + 2], b.v[j], c.v[j + 1], a.v[j + 1], k, rinv);
+            const int y = y0 + j;
+            if (wr && y < Y) out[x + y * X + z * XY] = o;
+        }
+    };
+
+    // set-up, consuming the input planes in increasing order: zs-2, zs-1, zs, zs+1
+    D2Rows<H> pm, p0, p1, p2, q0, q1, q2;
+    if (zs >= 2) load_plane(pm, zs - 2);
+    if (!stuck && zs >= 1) load_plane(p0, zs - 1);
+    if (!stuck) load_plane(p1, zs);
+    if (!stuck && zs + 1 < Z) load_plane(p2, zs + 1);
+    if (!stuck) {
+        if (zs < 1) ghost_plane(p0, p1, H + 4, y0 - 2);
+        if (zs + 1 >= Z) ghost_plane(p2, p1, H + 4, y0 - 2);
+        if (zs == 1) ghost_plane(pm, p0, H + 4, y0 - 2);
+        sweep1(q1, p0, p1, p2, zs);
+        if (zs >= 1) sweep1(q0, pm, p0, p1, zs - 1);
+        else ghost_plane(q0, q1, H + 2, y0 - 1);
+    }
+    // one march step for plane z: input plane z+2 into F and intermediate plane z+1 into QF, then
+    // the output plane z; the roles rotate through the three register sets (the loop is unrolled
+    // three times so that no values are copied)
+    auto step = [&](D2Rows<H>& A, D2Rows<H>& B, D2Rows<H>& F, D2Rows<H>& QA, D2Rows<H>& QB, D2Rows<H>& QF, int z) {
+        if (z + 1 < Z) {
+            if (z + 2 < Z) load_plane(F, z + 2); else ghost_plane(F, B, H + 4, y0 - 2);
+            if (stuck) return;
+            sweep1(QF, A, B, F, z + 1);
+        } else {
+            ghost_plane(QF, QB, H + 2, y0 - 1);
+        }
+        sweep2(QA, QB, QF, z);
+    };
+    int z = zs;
+    for (; !stuck && z + 2 < ze; z += 3) {
+        step(p1, p2, p0, q0, q1, q2, z);
+        if (stuck) break;
+        step(p2, p0, p1, q1, q2, q0, z + 1);
+        if (stuck) break;
+        step(p0, p1, p2, q2, q0, q1, z + 2);
+    }
+    if (!stuck && z < ze) {
+        step(p1, p2, p0, q0, q1, q2, z);
+        if (!stuck && z + 1 < ze) step(p2, p0, p1, q1, q2, q0, z + 1);
+    }
+    if (stuck && tid == 0) {
+        // record the timeout, then let the copies already issued land before the block's shared
+        // memory goes away (each wait again bounded)
+        sc->status = SKT_TIMEOUT;
+        for (int q = max(issued - D2SLOTS, 0); q < issued; ++q) (void)mbar_wait(&bar[q % D2SLOTS], unsigned(q / D2SLOTS) & 1u);
     }
 }
 
@@ -928,29 +1186,107 @@ namespace {
 // Flat terrain, X % 4 == 0: the sweeps alternate between the scratch fields and the last one
 // writes f itself, so no copy is needed (no sweep reads the array it writes, and the ground rows
 // of the scratch fields are never read). A single sweep goes through a scratch field.
+// z chunking of a march over gx x gy columns of blocks: about bps blocks per SM in the grid
+inline int z_runs(const Env& e, int gx, int gy, int bps, int& zlen) {
+    int zc = std::max(1, std::min(e.g.Z, (e.num_sms * bps + gx * gy - 1) / (gx * gy)));
+    zlen = (e.g.Z + zc - 1) / zc;
+    return (e.g.Z + zlen - 1) / zlen;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry points (no link against libcuda)
+typedef CUresult (*TensorMapEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                      const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+TensorMapEncodeFn tensor_map_encoder() {
+    static TensorMapEncodeFn fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<TensorMapEncodeFn>(p);
+    }
+    return fn;
+}
+
+// A field as a 3D tensor (x fastest) read in boxes of 36 x rows x 1 cells; false if it cannot be encoded.
+bool field_tensor_map(const Grid& g, const float* base, int rows, CUtensorMap* map) {
+    TensorMapEncodeFn enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {cuuint64_t(g.X), cuuint64_t(g.Y), cuuint64_t(g.Z)};
+    const cuuint64_t strides[2] = {cuuint64_t(g.X) * 4, cuuint64_t(g.XY) * 4};
+    const cuuint32_t box[3] = {cuuint32_t(D2BW), cuuint32_t(rows), 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool THETA, int H>
+bool launch_diffuse2(Env& e, int bps, const float* src, float* dst, int sides, int ground, const float* def, float k,
+                     const float* face) {
+    const Grid& g = e.g;
+    CUtensorMap map;
+    if (!field_tensor_map(g, src, d2_box_rows<H>(), &map)) return false;
+    const int gx = (g.X + D2OUT - 1) / D2OUT, gy = (g.Y - 1 + H * D2WARPS - 1) / (H * D2WARPS);
+    int zlen;
+    const int zc = z_runs(e, gx, gy, bps, zlen);
+    constexpr int smem = d2_smem_bytes<H>();
+    static bool attr = false;  // per template instance
+    if (!attr) {
+        cudaFuncSetAttribute(k_diffuse2<THETA, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+    }
+    k_diffuse2<THETA, H><<<dim3(gx, gy, zc), dim3(32, D2WARPS), smem, e.stream>>>(map, g, zlen, dst, sides, ground, def, k, face, e.sc);
+    return true;
+}
+
 void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float* def, float k, int sweeps) {
     const Grid& g = e.g;
     const int vx = (g.X / 4 + 31) / 32, vy = (g.Y - 1 + DVY - 1) / DVY;
-    int vz = std::max(1, std::min(g.Z, (e.num_sms * 32 + vx * vy - 1) / (vx * vy)));
-    const int vlen = (g.Z + vz - 1) / vz;
-    vz = (g.Z + vlen - 1) / vlen;
-    float* buf[2] = {e.tA, e.tB};
+    int vlen;
+    const int vz = z_runs(e, vx, vy, e.tune.diffuse_bps, vlen);
+    float* buf[3] = {e.tA, e.tB, e.As};  // As: the middle sweep of a pair when no tensor map can be made
     const float* src = f;
     float* face = e.g2a;  // ground scratch: free until the ground stage refills it
     if (type == 0) {
         k_theta_face<<<(g.X * g.Z + 255) / 256, 256, 0, e.stream>>>(g, e.p, e.Tg, e.Pg, face);
         e.launches += 1;
     }
-    for (int q = 0; q < sweeps; ++q) {
-        float* dst = (q == sweeps - 1 && q > 0) ? f : buf[q % 2];
-        if (type == 0)
+    // passes of one sweep, or (temporal blocking of depth 2) of two sweeps: an odd count starts
+    // with a single sweep
+    const bool pairs = e.tune.diffuse_depth == 2;
+    const int npass = pairs ? sweeps / 2 + sweeps % 2 : sweeps;
+    for (int q = 0; q < npass; ++q) {
+        float* dst = (q == npass - 1 && q > 0) ? f : buf[q % 2];
+        const bool two = pairs && !(q == 0 && sweeps % 2 == 1);
+        if (two) {
+            const int h = e.tune.diffuse_h, bps = e.tune.diffuse2_bps;
+            bool ok;
+            if (type == 0)
+                ok = h == 8 ? launch_diffuse2<true, 8>(e, bps, src, dst, sides, ground, def, k, face)
+                            : launch_diffuse2<true, 4>(e, bps, src, dst, sides, ground, def, k, face);
+            else
+                ok = h == 8 ? launch_diffuse2<false, 8>(e, bps, src, dst, sides, ground, def, k, nullptr)
+                            : launch_diffuse2<false, 4>(e, bps, src, dst, sides, ground, def, k, nullptr);
+            if (!ok) {  // no tensor-map encoder: the two sweeps as two passes
+                if (type == 0) {
+                    k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, buf[2], sides, ground, def, k, face);
+                    k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, buf[2], dst, sides, ground, def, k, face);
+                } else {
+                    k_diffuse4<false><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, buf[2], sides, ground, def, k, nullptr);
+                    k_diffuse4<false><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, buf[2], dst, sides, ground, def, k, nullptr);
+                }
+                e.launches += 1;
+            }
+        } else if (type == 0) {
             k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, face);
-        else
+        } else {
             k_diffuse4<false><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, dst, sides, ground, def, k, nullptr);
+        }
         e.launches += 1;
         src = dst;
     }
-    if (sweeps == 1) {
+    if (npass == 1) {
         const int n4 = g.N / 4;
         k_copy_sky4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)src, (float4*)f,
                                                                                      nullptr, 0);
@@ -1049,18 +1385,18 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     float* O = e.tA;
     const bool vec = e.flat && (g.X % 4) == 0;
     const int gx = (g.X / 4 + 31) / 32, gy = (g.Y - 1 + DVY - 1) / DVY;
-    int zc = std::max(1, std::min(g.Z, (e.num_sms * 16 + gx * gy - 1) / (gx * gy)));
+    int zc = std::max(1, std::min(g.Z, (e.num_sms * e.tune.ppm_bps + gx * gy - 1) / (gx * gy)));
     const int zlen = (g.Z + zc - 1) / zc;
     zc = (g.Z + zlen - 1) / zlen;
     const dim3 vg(gx, gy, zc), vb(32, DVY);
     // the Z pass marches: fewer, longer z chunks
-    int zc2 = std::max(1, std::min(g.Z, (e.num_sms * 8 + gx * gy - 1) / (gx * gy)));
+    int zc2 = std::max(1, std::min(g.Z, (e.num_sms * e.tune.ppmz_bps + gx * gy - 1) / (gx * gy)));
     const int zlen2 = (g.Z + zc2 - 1) / zc2;
     zc2 = (g.Z + zlen2 - 1) / zlen2;
     const dim3 vg2(gx, gy, zc2);
     // the Y pass marches rows in runs
     const int ygz = (g.Z + PY - 1) / PY;
-    int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * 32 + gx * ygz - 1) / (gx * ygz)));
+    int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * e.tune.ppmy_bps + gx * ygz - 1) / (gx * ygz)));
     const int ylen = (g.Y - 1 + yc - 1) / yc;
     yc = (g.Y - 1 + ylen - 1) / ylen;
     const dim3 yg(gx, ygz, yc), yb(32, PY);

@@ -10,6 +10,7 @@ through the C ABI of libskewt_gb300; errors raise ``SktError`` carrying the skt_
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 from enum import IntEnum
 from typing import Optional
@@ -312,6 +313,33 @@ class Environment:
         out = np.empty(self.ng, np.int32)
         self._check(self._L.skt_read_ground_height(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), out.size))
         return out
+
+    # -- launch-shape tuning ---------------------------------------------------------------------
+    TUNING_FIELDS = ("diffuse_depth", "diffuse_rows", "diffuse_bps", "diffuse2_bps", "ppm_x_bps", "ppm_y_bps", "ppm_z_bps")
+
+    def get_tuning(self) -> dict:
+        t = _lib.Tuning()
+        self._check(self._L.skt_get_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k in self.TUNING_FIELDS}
+
+    def set_tuning(self, **kw):
+        """Changes some launch shapes (keys of get_tuning()); the others stay."""
+        cur = self.get_tuning()
+        unknown = set(kw) - set(cur)
+        if unknown:
+            raise ValueError(f"unknown tuning keys {sorted(unknown)}")
+        cur.update(kw)
+        t = _lib.Tuning(*[int(cur[k]) for k in self.TUNING_FIELDS])
+        self._check(self._L.skt_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, cache_path=None, force=False) -> dict:
+        """skt_autotune: the launch shapes for this grid, from the cache file or measured."""
+        t = _lib.Tuning()
+        path = os.fsencode(cache_path) if cache_path else None
+        self._check(self._L.skt_autotune(self._h, path, 1 if force else 0, ctypes.byref(t)))
+        d = {k: getattr(t, k) for k in self.TUNING_FIELDS}
+        d.update(from_cache=bool(t.from_cache), diffuse_ms=t.diffuse_ms, advect_ms=t.advect_ms)
+        return d
 
     def read_neighbours(self) -> np.ndarray:
         """The Neigh records of every cell (computeNeighbourGPU's layout): uint8 (n, 6, 2) of
