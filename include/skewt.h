@@ -79,7 +79,13 @@ typedef struct {
     float refine_tol;   /* MIXED: relative residual target of the FP64 refinement (1e-8) */
     int inner_max_iter; /* MIXED: FP32 iterations per refinement step */
     float inner_rtol;   /* MIXED: relative tolerance of each FP32 inner solve */
-    int use_graph;      /* reserved, must be 0: the step is issued stream-ordered (no captured graph) */
+    int use_graph;      /* 1: each step is one launch of a CUDA graph captured at the first step (and
+                           again when dt, speed, the tuning, the diagnostics or the terrain's flatness
+                           change), its loops (advection substeps, PCG iterations, the mixed
+                           refinement) as conditional nodes decided on the device: no host
+                           synchronisation inside a step; the solver's status is read once per
+                           skt_step call. Not used while per-stage profiling is on. 0: launches
+                           issued stream-ordered, the loop counts read back by the host. */
     int mg_half;        /* MIXED: the V-cycle smooths with FP16 copies of the finest coefficients */
     int pcg_fused;      /* PLAIN, nx % 4 == 0: two launches per iteration (search step and pressure
                            update fused into the operator's march) instead of three; same values up

@@ -97,13 +97,11 @@ float* column_ptr(Env& e, int which) {
     }
 }
 
-// One step in the reference's stage order (Game/environment.cu:391-555).
-skt_status run_step(Env& e, float dt, float speed) {
+// The launches of one step in the reference's stage order (Game/environment.cu:391-555); the
+// ground kernel takes irr, or in graph mode reads it from the graph's first node.
+void queue_step(Env& e, float dt, float speed, float irr) {
     const float dtS = dt * speed;
     const bool hs = true;
-    const float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
-    // editorDataGPU at the start of updateGPU (Game/environment.cu:398): after a ground edit
-    if (e.ground_changed) launch_editor_block(e);
     // ground, then setTempsAtGround (fused into the ground column kernel)
     launch_ground(e, dt, speed, irr);
     // theta
@@ -139,15 +137,212 @@ skt_status run_step(Env& e, float dt, float speed) {
     e.last_nsub[9] = launch_advect(e, e.qi, e.zeroY, DIRICHLET, DIRICHLET, dtS, 9, hs, true);
     // microphysics + latent heat
     launch_micro(e, dt, speed);
-    // clock (m_time, Game/environment.cu:550-551)
+}
+
+// the host clock (m_time, Game/environment.cu:550-551)
+void advance_clock(Env& e, float dt, float speed) {
     e.sim_time += speed * dt * float(!e.pause);
     if (e.sim_time > 86400.0f) e.sim_time = 0.0f;
+}
+
+// One step in the reference's stage order (Game/environment.cu:391-555), stream-ordered.
+skt_status run_step(Env& e, float dt, float speed) {
+    const float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
+    // editorDataGPU at the start of updateGPU (Game/environment.cu:398): after a ground edit
+    if (e.ground_changed) launch_editor_block(e);
+    queue_step(e, dt, speed, irr);
+    advance_clock(e, dt, speed);
     return cuda_check(e, "step");
+}
+
+// ---- graph mode: the step captured once, its loops as conditional WHILE nodes ----------------
+
+__global__ void k_set_irr(float* dst, float irr) { *dst = irr; }
+
+#define GCHECK(call)                                                                  \
+    do {                                                                              \
+        const cudaError_t err_ = (call);                                              \
+        if (err_ != cudaSuccess && !e.graph_fail) {                                   \
+            e.graph_fail = true;                                                      \
+            e.graph_err = std::string(#call) + ": " + cudaGetErrorString(err_);        \
+        }                                                                             \
+    } while (0)
+
+Env::GraphKey graph_key(const Env& e, float dt, float speed) {
+    Env::GraphKey k{};
+    k.dt = dt;
+    k.speed = speed;
+    k.flat = e.flat;
+    k.rates_on = e.rates_on;
+    for (int i = 0; i < 3; ++i) {
+        k.rate_lo[i] = e.rates_on ? e.rate_lo[i] : 0;
+        k.rate_hi[i] = e.rates_on ? e.rate_hi[i] : 0;
+    }
+    k.diag_flags = e.diag_flags;
+    k.tune = e.tune;
+    return k;
+}
+bool same_key(const Env::GraphKey& a, const Env::GraphKey& b) {
+    const Tuning &s = a.tune, &t = b.tune;
+    return a.dt == b.dt && a.speed == b.speed && a.flat == b.flat && a.rates_on == b.rates_on && a.diag_flags == b.diag_flags &&
+           a.rate_lo[0] == b.rate_lo[0] && a.rate_lo[1] == b.rate_lo[1] && a.rate_lo[2] == b.rate_lo[2] && a.rate_hi[0] == b.rate_hi[0] &&
+           a.rate_hi[1] == b.rate_hi[1] && a.rate_hi[2] == b.rate_hi[2] && s.diffuse_depth == t.diffuse_depth && s.diffuse_h == t.diffuse_h &&
+           s.diffuse_bps == t.diffuse_bps && s.diffuse2_bps == t.diffuse2_bps && s.ppm_bps == t.ppm_bps && s.ppmy_bps == t.ppmy_bps &&
+           s.ppmz_bps == t.ppmz_bps;
+}
+
+void drop_graph(Env& e) {
+    if (e.graph_exec) cudaGraphExecDestroy(e.graph_exec);
+    if (e.graph) cudaGraphDestroy(e.graph);
+    e.graph_exec = nullptr;
+    e.graph = nullptr;
+    e.irr_node = nullptr;
+}
+
+// Captures one step (as queue_step queues it) into e.graph_exec.
+skt_status capture_step(Env& e, float dt, float speed) {
+    drop_graph(e);
+    for (int i = 0; i < 4; ++i)
+        if (!e.side[i] && cudaStreamCreateWithFlags(&e.side[i], cudaStreamNonBlocking) != cudaSuccess)
+            return fail(&e, SKT_CUDA_ERROR, "graph: side stream creation failed");
+    e.graph_fail = false;
+    e.graph_err.clear();
+    e.graph_loops = 0;
+    e.body_acc = 0;
+    e.graph_depth = 0;
+    const long long l0 = e.launches;
+    GCHECK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeRelaxed));
+    e.capturing = true;
+    e.irr_dev = &e.sc->irr;
+    k_set_irr<<<1, 1, 0, e.stream>>>(e.irr_dev, 0.0f);
+    e.launches += 1;
+    {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        GCHECK(cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+        e.irr_node = (nd == 1 && deps) ? deps[0] : nullptr;
+    }
+    queue_step(e, dt, speed, 0.0f);
+    cudaGraph_t graph = nullptr;
+    GCHECK(cudaStreamEndCapture(e.stream, &graph));
+    e.capturing = false;
+    const long long captured = e.launches - l0;
+    e.launches = l0;
+    e.graph = graph;
+    if (!e.graph_fail && !e.irr_node) {
+        e.graph_fail = true;
+        e.graph_err = "graph: the irradiance node was not found";
+    }
+    if (!e.graph_fail) GCHECK(cudaGraphInstantiate(&e.graph_exec, graph, 0));
+    if (e.graph_fail) {
+        cudaGetLastError();
+        const std::string m = e.graph_err;
+        drop_graph(e);
+        return fail(&e, SKT_CUDA_ERROR, m);
+    }
+    e.graph_static = captured - e.body_acc;
+    e.gkey = graph_key(e, dt, speed);
+    // the trip counters keep counting from where they stand
+    cudaMemcpyAsync(e.trips_seen, e.sc->trips, sizeof(e.trips_seen), cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+    return cuda_check(e, "graph capture");
+}
+
+// nsteps launches of the captured step; the host reads the solver scalars once at the end
+skt_status step_graph(Env& e, float dt, float speed, int nsteps) {
+    if (!e.graph_exec || !same_key(e.gkey, graph_key(e, dt, speed))) {
+        const skt_status st = capture_step(e, dt, speed);
+        if (st != SKT_OK) return st;
+    }
+    if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
+    cudaEventRecord(e.ev0, e.stream);
+    for (int i = 0; i < nsteps; ++i) {
+        if (e.ground_changed) launch_editor_block(e);  // after a ground edit, outside the graph
+        e.ground_changed = 0;
+        float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
+        cudaKernelNodeParams kp{};
+        void* args[2] = {&e.irr_dev, &irr};
+        kp.func = (void*)k_set_irr;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        kp.kernelParams = args;
+        if (cudaGraphExecKernelNodeSetParams(e.graph_exec, e.irr_node, &kp) != cudaSuccess) return cuda_check(e, "graph irradiance update");
+        if (cudaGraphLaunch(e.graph_exec, e.stream) != cudaSuccess) return cuda_check(e, "graph launch");
+        advance_clock(e, dt, speed);
+    }
+    cudaEventRecord(e.ev1, e.stream);
+    cudaEventSynchronize(e.ev1);
+    cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
+    const skt_status st = cuda_check(e, "graph step");
+    if (st != SKT_OK) return st;
+    fetch_scalars(e);
+    const Scalars& h = *e.host_sc;
+    long long ran = e.graph_static * nsteps;
+    for (int l = 0; l < e.graph_loops; ++l) {
+        ran += (long long)(h.trips[l] - e.trips_seen[l]) * e.loop_body[l];
+        e.trips_seen[l] = h.trips[l];
+    }
+    e.launches += ran;
+    for (int f = 0; f < 10; ++f) e.last_nsub[f] = h.nsub_f[f];
+    if (e.cfg.precision == 1) {
+        e.last_outer = h.outer;
+        e.last_iters = h.outer_inner_total;
+        e.last_residual = float(h.rnorm0 > 0 ? h.rnorm / h.rnorm0 : 0.0);
+        e.last_converged = h.refine_done == 1;
+    } else {
+        e.last_iters = h.iters;
+        e.last_residual = h.residual;
+        e.last_converged = h.converged == 1;
+    }
+    return SKT_OK;
 }
 
 }  // namespace
 
 namespace skt {
+void graph_while(Env& e, const std::function<void(cudaGraphConditionalHandle)>& init,
+                 const std::function<void(cudaGraphConditionalHandle, int)>& body) {
+    if (e.graph_loops >= kMaxGraphLoops || e.graph_depth >= 4) {
+        if (!e.graph_fail) {
+            e.graph_fail = true;
+            e.graph_err = "graph: too many or too deeply nested loops";
+        }
+        return;
+    }
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    GCHECK(cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphConditionalHandle h{};
+    GCHECK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    init(h);
+    GCHECK(cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    GCHECK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    GCHECK(cudaStreamUpdateCaptureDependencies(e.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    const int loop = e.graph_loops++;
+    cudaStream_t outer = e.stream, side = e.side[e.graph_depth++];
+    GCHECK(cudaStreamBeginCaptureToGraph(side, p.conditional.phGraph_out[0], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    e.stream = side;
+    const long long l0 = e.launches, acc0 = e.body_acc;
+    e.body_acc = 0;
+    body(h, loop);
+    const long long all = e.launches - l0;
+    e.loop_body[loop] = all - e.body_acc;  // this body's own kernels, nested bodies excluded
+    e.body_acc = acc0 + all;               // the enclosing level sees the whole body as looped
+    e.stream = outer;
+    cudaGraph_t done = nullptr;
+    GCHECK(cudaStreamEndCapture(side, &done));
+    e.graph_depth--;
+}
+
 void set_global_error(const char* msg) { g_create_err = msg ? msg : ""; }
 skt_status report(Env* e, skt_status st, const char* msg) { return fail(e, st, msg); }
 float* field_ptr(Env& e, int param, int dir) { return sky_ptr(e, param, dir); }
@@ -278,7 +473,7 @@ skt_status skt_create(const skt_grid_desc* grid, const skt_solver_cfg* cfg, skt_
     if (c.diffuse_sweeps < 0 || c.pcg_max_iter < 0 || c.max_substeps < 1 || (c.semantics != 0 && c.semantics != 1) ||
         (c.precision != 0 && c.precision != 1))
         return fail(nullptr, SKT_INVALID_ARG, "invalid solver configuration");
-    if (c.use_graph != 0) return fail(nullptr, SKT_INVALID_ARG, "use_graph is reserved: the step is not captured as a CUDA graph");
+    if (c.use_graph != 0 && c.use_graph != 1) return fail(nullptr, SKT_INVALID_ARG, "use_graph must be 0 or 1");
     skt_env* h = new (std::nothrow) skt_env();
     if (!h) return fail(nullptr, SKT_OUT_OF_MEMORY, "host allocation failed");
     Env& e = h->e;
@@ -388,6 +583,9 @@ void skt_destroy(skt_env* env) {
     if (e.copy_stream) cudaStreamDestroy(e.copy_stream);
     if (e.brick_flags) cudaFree(e.brick_flags);
     if (e.brick_out) cudaFree(e.brick_out);
+    drop_graph(e);
+    for (cudaStream_t side : e.side)
+        if (side) cudaStreamDestroy(side);
     if (e.host_sc) cudaFreeHost(e.host_sc);
     if (e.stream) cudaStreamDestroy(e.stream);
     delete env;
@@ -434,6 +632,22 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     Env& e = env->e;
     if (!e.initialized) return fail(&e, SKT_NOT_INITIALIZED, "skt_init has not run");
     if (!(dt > 0.0f) || !(speed > 0.0f) || nsteps < 0) return fail(&e, SKT_INVALID_ARG, "dt and speed must be > 0, nsteps >= 0");
+    if (e.cfg.use_graph && !e.prof && nsteps > 0) {
+        // graph mode: the status is read once after the nsteps launches
+        const skt_status gs = step_graph(e, dt, speed, nsteps);
+        if (gs != SKT_OK) return gs;
+        const int dev_status = e.host_sc->status;
+        if (dev_status != 0) {
+            cudaMemsetAsync(&e.sc->status, 0, sizeof(int), e.stream);
+            cudaStreamSynchronize(e.stream);
+            e.host_sc->status = 0;
+            return fail(&e, skt_status(dev_status),
+                        dev_status == SKT_TIMEOUT ? "a kernel's wait for its streamed data ran out (the state is not valid)"
+                                                  : "a step of this call met a NaN or Inf (in the wind or in a pressure-solver "
+                                                    "reduction: a non-finite field value or a zero-density cell); the state is not valid");
+        }
+        return e.last_converged ? SKT_OK : SKT_NOT_CONVERGED;
+    }
     skt_status worst = SKT_OK;
     if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
     cudaEventRecord(e.ev0, e.stream);
@@ -460,9 +674,11 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
         cudaStreamSynchronize(e.stream);
         e.host_sc->status = 0;
         return fail(&e, skt_status(dev_status),
-                    "step " + std::to_string(done) + " of this call met a NaN or Inf (in the wind or in a pressure-solver "
-                    "reduction: a non-finite field value or a zero-density cell); the remaining steps were not run and "
-                    "the state is not valid");
+                    dev_status == SKT_TIMEOUT
+                        ? "step " + std::to_string(done) + " of this call: a kernel's wait for its streamed data ran out (the state is not valid)"
+                        : "step " + std::to_string(done) + " of this call met a NaN or Inf (in the wind or in a pressure-solver "
+                          "reduction: a non-finite field value or a zero-density cell); the remaining steps were not run and "
+                          "the state is not valid");
     }
     return worst;
 }

@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "skt_physics.cuh"
@@ -64,6 +65,8 @@ __device__ __forceinline__ float face_nb(const Grid& g, const float* __restrict_
     return q[cidx(g, xn, yn, zn)];
 }
 
+constexpr int kMaxGraphLoops = 16;  // conditional loops of one captured step
+
 // Device-resident scalars of the solver (one per environment).
 struct Scalars {
     double sigma0, sigma1, beta;      // PCG scalars (FP64)
@@ -84,6 +87,11 @@ struct Scalars {
     int outer_inner_total;            // mixed mode: inner iterations summed over the refinement
     int refine_done;                  // mixed mode: relative FP64 residual met refine_tol
     int edit_changed;                 // an edit changed the ground store
+    // graph mode (the step captured as a CUDA graph, conditional nodes for the loops)
+    float irr;                        // the step's irradiance, set by the graph's first node
+    int slot;                         // advection: substeps done in the current field's loop
+    int nsub_f[10];                   // advection: substep count of each field in the last step
+    unsigned int trips[kMaxGraphLoops];  // completed trips of each captured loop body (cumulative)
 };
 
 // A non-finite total of a solver reduction (a dot product or squared norm over every sky cell)
@@ -179,6 +187,26 @@ struct Env {
     int num_sms = 148;
     std::string err;
     int flat = 1;  // all gh == 0
+    // graph mode: the step captured once per key, the loops as conditional WHILE nodes
+    bool capturing = false;              // launches go into a stream capture (no host reads)
+    cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};  // capture streams of nested loop bodies
+    int graph_depth = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphNode_t irr_node = nullptr;  // the node that stores the step's irradiance (updated per launch)
+    float* irr_dev = nullptr;            // the irradiance the ground kernel reads in graph mode
+    struct GraphKey {
+        float dt, speed;
+        int flat, rates_on, rate_lo[3], rate_hi[3], diag_flags;
+        Tuning tune;
+    } gkey{};
+    long long graph_static = 0;          // kernels of one launch outside the loop bodies
+    int graph_loops = 0;                 // loops captured
+    long long loop_body[kMaxGraphLoops] = {0};  // kernels of one trip of each loop body (nested bodies excluded)
+    unsigned int trips_seen[kMaxGraphLoops] = {0};
+    long long body_acc = 0;              // capture bookkeeping: kernels inside loop bodies at the current level
+    bool graph_fail = false;             // a capture call failed
+    std::string graph_err;
     // graph
     // multigrid hierarchy of the mixed-precision solve (level 0 = the grid itself)
     int mg_levels = 0;
@@ -219,10 +247,10 @@ struct ProfScope {
     cudaEvent_t a = nullptr;
     long long l0;
     ProfScope(Env& env, const char* n) : e(env), name(n), l0(env.launches) {
-        if (e.prof) { cudaEventCreate(&a); cudaEventRecord(a, e.stream); }
+        if (e.prof && !e.capturing) { cudaEventCreate(&a); cudaEventRecord(a, e.stream); }
     }
     ~ProfScope() {
-        if (e.prof) {
+        if (e.prof && !e.capturing) {
             cudaEvent_t b;
             cudaEventCreate(&b);
             cudaEventRecord(b, e.stream);
@@ -247,6 +275,14 @@ void launch_init_state(Env& e, int noise, uint32_t seed);
 void launch_isen_ground(Env& e);  // computeIsenTempGroundGPU on the current heightfield
 void launch_editor_block(Env& e);  // editorDataGPU's ground block (after a ground edit)
 bool mg_allocate(Env& e);
+// Graph capture: inside a capture of e.stream, adds a WHILE conditional node. `init` queues the
+// kernel that sets the node's condition for the first trip (before the node); `body` queues the
+// body's launches (e.stream then points at a side stream that captures into the node's body graph)
+// and must end with a kernel that counts the trip (note_trip) and sets the condition again. Both get
+// the node's handle; body also gets the loop's index into Scalars::trips.
+void graph_while(Env& e, const std::function<void(cudaGraphConditionalHandle)>& init,
+                 const std::function<void(cudaGraphConditionalHandle, int)>& body);
+__device__ __forceinline__ void note_trip(Scalars* sc, int loop) { sc->trips[loop] += 1; }
 void launch_matvec_textbook(Env& e, const float* s, float* As);
 void mg_solve(Env& e);
 

@@ -1172,6 +1172,129 @@ void vcycle_vec(Env& e, int l, const CT* ax, const CT* ay, const CT* az, const C
 
 }  // namespace
 
+// graph mode, refinement loop: another refinement step while the relative residual is above the
+// target, no NaN was met and the step cap is not reached (loop < 0: the loop's start)
+__global__ void k_outer_cond(cudaGraphConditionalHandle h, Scalars* sc, int loop, int max_outer) {
+    if (loop < 0) {
+        sc->outer = 0;
+    } else {
+        note_trip(sc, loop);
+        sc->outer += 1;
+    }
+    cudaGraphSetConditional(h, (sc->refine_done != 1 && sc->status == 0 && sc->outer < max_outer) ? 1u : 0u);
+}
+// graph mode, inner CG loop: another chunk of iterations while the inner solve has not stopped
+__global__ void k_inner_cond(cudaGraphConditionalHandle h, Scalars* sc, int loop) {
+    if (loop >= 0) note_trip(sc, loop);
+    cudaGraphSetConditional(h, (sc->converged == 0 && sc->status == 0) ? 1u : 0u);
+}
+
+// The refinement as captured graph nodes: the first residual, then a WHILE loop of refinement steps
+// (inner solve, correction, residual), each inner solve a WHILE loop of chunks of four CG
+// iterations. The same kernels in the same order as mg_solve's stream-ordered loop; the stop tests
+// run on the device instead of the host. sc->outer counts the refinement steps.
+void mg_solve_graph(Env& e, bool fused, int max_outer, float* bvec, float* ecor, float* z0, float* z0b, float* xh, float* xl, int nb) {
+    const Grid& g = e.g;
+    const int n = g.N;
+    auto resid = [&](int first) {
+        ProfScope ps(e, "mg_refine");
+        if (fused) {
+            const March m = march(e, g.X, g.Y, g.Z);
+            k_resid_ff4<<<m.grid, dim3(32, JVY), 0, e.stream>>>(g.X, g.Y, g.Z, m.zlen, e.ax, e.ay, e.az, e.aw, xh, xl, bvec, e.r,
+                                                              e.cfg.refine_tol, first, e.sc, e.partials);
+        } else {
+            k_resid_ff<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, xh, xl, bvec, e.r, e.cfg.refine_tol, first, e.sc, e.partials);
+        }
+        e.launches += 1;
+    };
+    const int* conv = &e.sc->converged;
+    auto inner = [&]() {
+        if (fused) {
+            { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, nullptr, DOT_START); }
+            const March m = march(e, g.X, g.Y, g.Z);
+            graph_while(
+                e, [&](cudaGraphConditionalHandle h) {
+                    k_inner_cond<<<1, 1, 0, e.stream>>>(h, e.sc, -1);
+                    e.launches += 1;
+                },
+                [&](cudaGraphConditionalHandle h, int loop) {
+                    float* s_old = e.s;
+                    float* s_new = e.pp;
+                    for (int k = 0; k < 4; ++k) {  // an even count: the buffers' roles repeat every trip
+                        { ProfScope ps(e, "mg_matvec");
+                          k_mg_matvec_search4<<<m.grid, dim3(32, JVY), 0, e.stream>>>(g.X, g.Y, g.Z, m.zlen, e.ax, e.ay, e.az, e.aw, z0,
+                                                                                    s_old, s_new, e.As, e.sc, e.partials);
+                          e.launches += 1; }
+                        { ProfScope ps(e, "mg_update");
+                          k_update_mg4<<<nb, RT, 0, e.stream>>>(n / 4, (const float4*)s_new, (const float4*)e.As, (float4*)ecor,
+                                                               (float4*)e.r, e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials);
+                          e.launches += 1; }
+                        { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NEXT); }
+                        std::swap(s_old, s_new);
+                    }
+                    k_inner_cond<<<1, 1, 0, e.stream>>>(h, e.sc, loop);
+                    e.launches += 1;
+                });
+            return;
+        }
+        { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, nullptr, DOT_NONE); }
+        const bool vec = (g.X % 4) == 0;
+        const int n4 = n / 4;
+        if (vec) k_zr4<true><<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (const float4*)e.r, (float4*)e.s, e.sc, e.partials);
+        else k_zr_search<true><<<nb, RT, 0, e.stream>>>(n, z0, e.r, e.s, e.sc, e.partials);
+        e.launches += 1;
+        graph_while(
+            e, [&](cudaGraphConditionalHandle h) {
+                k_inner_cond<<<1, 1, 0, e.stream>>>(h, e.sc, -1);
+                e.launches += 1;
+            },
+            [&](cudaGraphConditionalHandle h, int loop) {
+                for (int k = 0; k < 4; ++k) {
+                    if (vec) {
+                        { ProfScope ps(e, "mg_matvec"); launch_matvec_textbook(e, e.s, e.As); }
+                        { ProfScope ps(e, "mg_update");
+                          k_update_mg4<<<nb, RT, 0, e.stream>>>(n4, (const float4*)e.s, (const float4*)e.As, (float4*)ecor, (float4*)e.r,
+                                                               e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials); }
+                        { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NONE); }
+                        { ProfScope ps(e, "mg_search");
+                          k_zr4<false><<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (const float4*)e.r, nullptr, e.sc, e.partials);
+                          k_search_mg4<<<nb, RT, 0, e.stream>>>(n4, (const float4*)z0, (float4*)e.s, e.sc); }
+                        e.launches += 3;
+                        continue;
+                    }
+                    { ProfScope ps(e, "mg_matvec");
+                      k_matvec_mg<<<nb, RT, 0, e.stream>>>(g, e.ax, e.ay, e.az, e.aw, e.s, e.As, e.sc, e.partials); }
+                    { ProfScope ps(e, "mg_update");
+                      k_update_mg<<<nb, RT, 0, e.stream>>>(n, e.s, e.As, ecor, e.r, e.cfg.inner_rtol, e.cfg.inner_max_iter, e.sc, e.partials); }
+                    { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, conv, DOT_NONE); }
+                    { ProfScope ps(e, "mg_search");
+                      k_zr_search<false><<<nb, RT, 0, e.stream>>>(n, z0, e.r, e.s, e.sc, e.partials);
+                      k_search_mg<<<nb, RT, 0, e.stream>>>(n, z0, e.s, e.sc); }
+                    e.launches += 4;
+                }
+                k_inner_cond<<<1, 1, 0, e.stream>>>(h, e.sc, loop);
+                e.launches += 1;
+            });
+    };
+    resid(1);
+    graph_while(
+        e, [&](cudaGraphConditionalHandle h) {
+            k_outer_cond<<<1, 1, 0, e.stream>>>(h, e.sc, -1, max_outer);
+            e.launches += 1;
+        },
+        [&](cudaGraphConditionalHandle h, int loop) {
+            inner();
+            { ProfScope ps(e, "mg_refine");
+              k_accum_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, ecor);
+              e.launches += 1; }
+            resid(0);
+            k_outer_cond<<<1, 1, 0, e.stream>>>(h, e.sc, loop, max_outer);
+            e.launches += 1;
+        });
+    k_cast_ff<<<nb, RT, 0, e.stream>>>(n, xh, xl, e.pp);
+    e.launches += 1;
+}
+
 // Solves A p = b (b = the divergence in e.r on entry, A from k_build in textbook form) into
 // e.pp. Uses e.tA (b), e.tB (inner correction), e.r/e.s/e.As (inner CG) and e.rd (V-cycle
 // vectors). Returns after the refinement met refine_tol or the outer cap.
@@ -1196,6 +1319,10 @@ void mg_solve(Env& e) {
     const bool fused = e.mg_levels > 0 && vec_level(e, 0);
     int outer = 0;
     const int max_outer = 12;
+    if (e.capturing) {
+        mg_solve_graph(e, fused, max_outer, bvec, ecor, z0, z0b, xh, xl, nb);
+        return;
+    }
     for (; outer < max_outer; ++outer) {
         {
             ProfScope ps(e, "mg_refine");

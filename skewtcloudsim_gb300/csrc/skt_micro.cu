@@ -255,9 +255,12 @@ struct GroundPtrs {
 // (calculatePrecipHittingGroundMicroPhysicsGPU Game/microPhysics.cu:1544), ground
 // microphysics (calculateGroundMicroPhysicsGPU :1419) and the relaxation of the first sky cell
 // towards the ground potential temperature (setTempsAtGroundGPU Game/kernelSky.cu:255).
-__global__ void k_ground_column(Grid g, GroundPtrs P, float dt, float speed, float irr, Micro M) {
+// irr_dev: in graph mode the irradiance is read from device memory (the graph's first node writes
+// it); otherwise irr is used
+__global__ void k_ground_column(Grid g, GroundPtrs P, float dt, float speed, float irr_arg, const float* __restrict__ irr_dev, Micro M) {
     const int idxG = blockIdx.x * blockDim.x + threadIdx.x;
     if (idxG >= g.X * g.Z) return;
+    const float irr = irr_dev ? *irr_dev : irr_arg;
     const int x = idxG % g.X, z = idxG / g.X;
     const int gh = g.gh[idxG];
     const float vox = g.vox;
@@ -441,7 +444,7 @@ void launch_ground(Env& e, float dt, float speed, float irr) {
     GroundPtrs P{e.qv, e.qw, e.qc, e.qr, e.qs, e.qi, e.th, e.rho, e.p, e.u, e.Qrs, e.Qgr, e.Qgs, e.Qgi, e.Pg, e.tg, e.Tg, e.cover};
     Micro M;
     M.G = e.gam;
-    k_ground_column<<<(n2 + 127) / 128, 128, 0, e.stream>>>(g, P, dt, speed, irr, M);
+    k_ground_column<<<(n2 + 127) / 128, 128, 0, e.stream>>>(g, P, dt, speed, irr, e.capturing ? e.irr_dev : nullptr, M);
 }
 
 void launch_isen_ground(Env& e) {

@@ -688,6 +688,31 @@ __global__ void __launch_bounds__(UT) k_pressure_tail4(int n4, const float4* __r
     }
 }
 
+// graph mode: the last iteration's pressure update from the direction buffer of its parity
+__global__ void __launch_bounds__(UT) k_pressure_tail_sel(int n4, const float4* __restrict__ s0, const float4* __restrict__ s1,
+                                                          float4* __restrict__ pp, const Scalars* sc) {
+    const int it = sc->iters;
+    if (it <= 0) return;
+    const float4* __restrict__ s = ((it - 1) & 1) ? s1 : s0;
+    const float alpha = sc->alpha_pp;
+    for (int i = blockIdx.x * UT + threadIdx.x; i < n4; i += gridDim.x * UT) {
+        const float4 sv = s[i];
+        float4 pv = pp[i];
+        pv.x = __fmaf_rn(alpha, sv.x, pv.x);
+        pv.y = __fmaf_rn(alpha, sv.y, pv.y);
+        pv.z = __fmaf_rn(alpha, sv.z, pv.z);
+        pv.w = __fmaf_rn(alpha, sv.w, pv.w);
+        pp[i] = pv;
+    }
+}
+
+// graph mode, PCG loop: run (another) chunk of iterations while the solver has not stopped and no
+// NaN was met; loop >= 0 counts a completed trip
+__global__ void k_pcg_cond(cudaGraphConditionalHandle h, Scalars* sc, int loop) {
+    if (loop >= 0) note_trip(sc, loop);
+    cudaGraphSetConditional(h, (sc->converged == 0 && sc->status == 0) ? 1u : 0u);
+}
+
 // k_build for flat terrain and X % 4 == 0: four cells per thread, a march along z in blocks of
 // MVY rows. Each cell's reciprocal density is formed once (the x neighbours' by shuffle, the next
 // plane's carried), and each face once: a cell forms its right, up and front faces; the left face
@@ -1001,11 +1026,9 @@ void launch_project(Env& e, float dtS) {
     // dirs[k % 2]
     float* dirs[2] = {e.s, e.tB};
     float* zbuf = e.tA;
-    for (int it = 0; it < e.cfg.pcg_max_iter; it += chunk) {
-        const int n = std::min(chunk, e.cfg.pcg_max_iter - it);
-        for (int k = 0; k < n; ++k) {
+    // iteration kk of the PCG (directions alternate between the two buffers in the fused form)
+    auto iterate = [&](int kk) {
             if (vec && e.cfg.pcg_fused) {
-                const int kk = it + k;
                 float* sd = dirs[kk & 1];
                 { ProfScope ps(e, "pcg_matvec"); e.launches += 1;
                   if (kk == 0) {  // the first direction is z itself (set by the build)
@@ -1037,7 +1060,33 @@ void launch_project(Env& e, float dtS) {
                 { ProfScope ps(e, "pcg_update"); e.launches += 1; k_update<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.s, e.As, e.pp, e.r, ref, e.cfg.pcg_tol, e.cfg.pcg_max_iter, e.sc, e.partials); }
                 { ProfScope ps(e, "pcg_search"); e.launches += 1; k_search<<<nblk, NT, 0, e.stream>>>(g, T, e.aw, e.r, e.s, e.sc); }
             }
+    };
+    if (e.capturing) {
+        // graph mode: iteration 0, then chunks of `chunk` iterations as a WHILE loop that runs while
+        // the solver has not stopped (an even chunk keeps the direction buffers' parity); the
+        // kernels of iterations past the stop return at once, as in the stream-ordered form
+        if (e.cfg.pcg_max_iter > 0) {
+            iterate(0);
+            graph_while(
+                e, [&](cudaGraphConditionalHandle h) {
+                    k_pcg_cond<<<1, 1, 0, e.stream>>>(h, e.sc, -1);
+                    e.launches += 1;
+                },
+                [&](cudaGraphConditionalHandle h, int loop) {
+                    for (int kk = 1; kk <= chunk; ++kk) iterate(kk);
+                    k_pcg_cond<<<1, 1, 0, e.stream>>>(h, e.sc, loop);
+                    e.launches += 1;
+                });
+            if (vec && e.cfg.pcg_fused) {
+                ProfScope ps(e, "pcg_update");
+                e.launches += 1;
+                k_pressure_tail_sel<<<nstream, UT, 0, e.stream>>>(n4, (const float4*)dirs[0], (const float4*)dirs[1], (float4*)e.pp, e.sc);
+            }
         }
+    } else {
+    for (int it = 0; it < e.cfg.pcg_max_iter; it += chunk) {
+        const int n = std::min(chunk, e.cfg.pcg_max_iter - it);
+        for (int k = 0; k < n; ++k) iterate(it + k);
         fetch_scalars(e);
         if (e.host_sc->converged || e.host_sc->status != 0) break;
     }
@@ -1050,6 +1099,7 @@ void launch_project(Env& e, float dtS) {
     e.last_iters = e.host_sc->iters;
     e.last_residual = e.host_sc->residual;
     e.last_converged = e.host_sc->converged == 1;
+    }
     }
     const dim3 grd((g.X + 31) / 32, (g.Y + 7) / 8, g.Z), blk(32, 8);
     ProfScope ps(e, "proj_apply");

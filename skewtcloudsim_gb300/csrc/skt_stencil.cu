@@ -1341,6 +1341,19 @@ void launch_diffuse(Env& e, float* f, int type, float dtS) {
     }
 }
 
+// Graph mode, advection loop: the first trip runs when the field has any substep; each trip counts
+// a substep and runs again while substeps remain. The field's count is kept for the step's stats.
+__global__ void k_adv_begin(cudaGraphConditionalHandle h, Scalars* sc, int field) {
+    sc->slot = 0;
+    if (field >= 0 && field < 10) sc->nsub_f[field] = sc->nsub;
+    cudaGraphSetConditional(h, sc->nsub > 0 ? 1u : 0u);
+}
+__global__ void k_adv_next(cudaGraphConditionalHandle h, Scalars* sc, int loop) {
+    note_trip(sc, loop);
+    sc->slot += 1;
+    cudaGraphSetConditional(h, sc->slot < sc->nsub ? 1u : 0u);
+}
+
 // advectPPMWGPU Game/environment.cu:692-824. With host_sync the substep count is read back as
 // the reference does; otherwise max_substeps slots are launched and the ones beyond the device
 // count exit at once (graph capture). Returns the substep count (or -1 when not read back).
@@ -1363,7 +1376,7 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
         }
         k_nsub<<<1, 1, 0, e.stream>>>(e.sc, dtS, g.vox, float(e.cfg.max_substeps));
         e.adv_nsub = -1;
-        if (host_sync) {
+        if (host_sync && !e.capturing) {
             fetch_scalars(e);
             e.adv_nsub = e.host_sc->nsub;
         } else {
@@ -1402,8 +1415,9 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     const dim3 yg(gx, ygz, yc), yb(32, PY);
     const int n4 = g.N / 4;
     const int ncopy = std::min((n4 + 255) / 256, e.num_sms * 8);
-    e.launches += 6LL * slots;
-    for (int i = 0; i < slots; ++i) {
+    // one substep (slot i; with chk set, the kernels read the substep count from the device and
+    // slots at or beyond it return at once)
+    auto substep = [&](int i, const Scalars* chk) {
         if (vec && f != e.v) {
             // A -> O -> B -> O -> B -> A through the second scratch field: the last pass writes the
             // field's sky cells itself (no copy). A pass reads the wind as it stands: for u (x
@@ -1414,7 +1428,7 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
             k_ppm4z<<<vg2, vb, 0, e.stream>>>(g, zlen2, B, O, f == e.w ? B : e.w, def, sides, e.defW, dtS, nsub, 0, chk, i);
             k_ppm4y<<<yg, yb, 0, e.stream>>>(g, ylen, O, B, e.v, def, sides, ground, dtS, nsub, 1, chk, i);
             k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, B, A, f == e.u ? B : e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
-            continue;
+            return;
         }
         if (vec) {
             k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
@@ -1433,7 +1447,7 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
             k_ppm4y<<<yg, yb, 0, e.stream>>>(g, ylen, O, A, vy, def, sides, ground, dtS, nsub, 1, chk, i);
             k_ppm4x<<<vg, vb, 0, e.stream>>>(g, zlen, A, O, e.u, def, sides, e.defU, dtS, nsub, 1, chk, i);
             k_copy_sky4<<<ncopy, 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)O, (float4*)A, chk, i);
-            continue;
+            return;
         }
         // pass 1: X half, A -> O (velocity u as it stands: for f == u this is A)
         k_ppm<0><<<grd, blk, 0, e.stream>>>(g, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
@@ -1456,7 +1470,25 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
         // pass 5: X half, A -> O, then A = O on sky cells
         k_ppm<0><<<grd, blk, 0, e.stream>>>(g, A, O, e.u, def, sides, ground, e.defU, e.defW, dtS, nsub, 1, chk, i);
         k_copy_sky<<<grd, blk, 0, e.stream>>>(g, O, A, chk, i);
+    };
+    if (e.capturing) {
+        // graph mode: the substep count stays on the device and the substeps run as a WHILE loop
+        e.adv_nsub = 0;
+        graph_while(
+            e, [&](cudaGraphConditionalHandle h) {
+                k_adv_begin<<<1, 1, 0, e.stream>>>(h, e.sc, slot_id);
+                e.launches += 1;
+            },
+            [&](cudaGraphConditionalHandle h, int loop) {
+                e.launches += 6;
+                substep(0, e.sc);
+                k_adv_next<<<1, 1, 0, e.stream>>>(h, e.sc, loop);
+                e.launches += 1;
+            });
+        return -1;
     }
+    e.launches += 6LL * slots;
+    for (int i = 0; i < slots; ++i) substep(i, chk);
     (void)slot_id;
     return nsub;
 }

@@ -115,7 +115,7 @@ class SolverConfig:
     refine_tol: float = 1e-8
     inner_max_iter: int = 60
     inner_rtol: float = 1e-4
-    use_graph: int = 0          # reserved: must be 0 (no captured graph)
+    use_graph: int = 0          # 1: each step is one launch of a captured CUDA graph
     mg_half: int = 1            # mixed: FP16 finest-level coefficients inside the V-cycle
     pcg_fused: int = 1          # plain: search step and pressure update fused into the operator
 
