@@ -257,11 +257,12 @@ TEXTBOOK_MAX_ITER = 20000
 
 def mode_config(args, mode):
     from skewtcloudsim_gb300 import SolverConfig
+    g = args.graph
     if mode == "plain":
-        return SolverConfig(semantics=args.semantics, precision=0, mg_half=args.mg_half, pcg_fused=args.pcg_fused)
+        return SolverConfig(semantics=args.semantics, precision=0, mg_half=args.mg_half, pcg_fused=args.pcg_fused, use_graph=g)
     if mode == "plain_textbook":
-        return SolverConfig(semantics=1, precision=0, pcg_max_iter=TEXTBOOK_MAX_ITER, pcg_fused=args.pcg_fused)
-    return SolverConfig(semantics=1, precision=1, mg_half=args.mg_half, pcg_fused=args.pcg_fused)
+        return SolverConfig(semantics=1, precision=0, pcg_max_iter=TEXTBOOK_MAX_ITER, pcg_fused=args.pcg_fused, use_graph=g)
+    return SolverConfig(semantics=1, precision=1, mg_half=args.mg_half, pcg_fused=args.pcg_fused, use_graph=g)
 
 
 def survey_step_bytes(mode, pcg_iters, outer):
@@ -333,18 +334,36 @@ def run_ensemble(args, rank, world, local, pg, torch):
         envs.append(env)
     dts = [m[1] for m in members]
     cells = sum(m[0].n for m in members)
-    step_ensemble(envs, dts, 1.0, nsteps=args.warmup)
+    from skewtcloudsim_gb300 import Ensemble
+    ens = Ensemble(envs) if args.ensemble_runner == "graph" else None
+
+    def advance(k):
+        if ens is not None:
+            ens.step(dts, 1.0, nsteps=k)
+        else:
+            step_ensemble(envs, dts, 1.0, nsteps=k)
+
+    advance(args.warmup)
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
     l0 = sum(e.stats()["kernel_launches"] for e in envs)
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        step_ensemble(envs, dts, 1.0, nsteps=args.steps)
+        advance(args.steps)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
     launches = sum(e.stats()["kernel_launches"] for e in envs) - l0
     el = t1 - t0
+    # the other runner on the same members, for comparison
+    other = None
+    if ens is not None:
+        torch.cuda.synchronize()
+        o0 = time.perf_counter()
+        step_ensemble(envs, dts, 1.0, nsteps=args.steps)
+        torch.cuda.synchronize()
+        other = (time.perf_counter() - o0) / args.steps * 1e3
+        ens.close()
     if pg:
         t = torch.tensor([el], device="cuda")
         pg.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -366,7 +385,10 @@ def run_ensemble(args, rank, world, local, pg, torch):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "members": n, "cells": cells, "pcg": "mixed" if prec else "plain",
                        "sizes": sorted({f"{m[0].nx}x{m[0].nz}x{m[0].ny}" for m in members}),
-                       "concurrency": "one host thread per member, one stream per member",
+                       "concurrency": ("one CUDA graph launch per ensemble step, every member's whole step an independent "
+                                       "branch (loops as device-side conditional nodes)" if ens is not None
+                                       else "one host thread per member, one stream per member"),
+                       "host_thread_runner_ms_per_step": other,
                        "sequential_ms_per_step": seq * 1e3, "parallelism": "single" if world == 1 else f"replicas{world}"},
             "gpu_launches": launches, "clocks": clk.summary()}), flush=True)
     return 0
@@ -385,6 +407,10 @@ def main():
     ap.add_argument("--mg-half", type=int, default=1, help="mixed: FP16 finest-level coefficients in the V-cycle")
     ap.add_argument("--pcg-fused", type=int, default=1,
                     help="plain: 1 = two launches per PCG iteration (search step fused into the operator), 0 = three")
+    ap.add_argument("--graph", type=int, default=1,
+                    help="1 = each step one launch of the captured CUDA graph (device-side loops), 0 = stream-ordered")
+    ap.add_argument("--ensemble-runner", default="graph", choices=["graph", "threads"],
+                    help="ensemble workloads: one graph launch per step for all members, or a host thread per member")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--shape", default=None, help="x,y,z (z vertical) override of the workload size")
@@ -449,9 +475,7 @@ def main():
         host_in = {k: pinned_like(getattr(init, k)) for k in ("theta", "vel", "qv", "ground_T", "ground_p", "p3d",
                                                                "p_column")}
         outs = {k: pinned_like(np.empty(cells, np.float32)) for k in names}
-        sem = args.semantics if head["mode"] == "plain" else 1
-        cfg = SolverConfig(semantics=sem, precision=1 if head["mode"] == "mixed" else 0, mg_half=args.mg_half,
-                       pcg_fused=args.pcg_fused)
+        cfg = mode_config(args, head["mode"])
         env2 = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
         K = args.steps
         torch.cuda.synchronize()

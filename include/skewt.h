@@ -146,6 +146,23 @@ skt_status skt_sync(skt_env* env);
 skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float dt0, const float* speed, int nsteps,
                              int threads, int* statuses);
 
+/* Ensemble as one CUDA graph (no counterpart in the reference, which runs one environment): every
+ * member's whole step, its loops as conditional nodes decided on the device, is captured as an
+ * independent branch of one graph at the first skt_ensemble_step (and again when a member's dt,
+ * speed, tuning, diagnostics or terrain flatness change), so each ensemble step is a single graph
+ * launch from the calling thread: the GPU runs the members' kernels side by side and the host
+ * synchronises once per call. Results equal stepping the members one by one, bit for bit. Members
+ * keep their own state and may still be stepped alone; they must outlive the ensemble and must
+ * not be stepped from another thread while the ensemble steps. */
+typedef struct skt_ensemble skt_ensemble;
+skt_status skt_ensemble_create(skt_env* const* envs, int n, skt_ensemble** out);
+void skt_ensemble_destroy(skt_ensemble* ens);
+/* nsteps steps of every member (dt and speed per member, or dt0 and 1 for all when NULL).
+ * Returns SKT_OK, or the first member's failure (SKT_NOT_CONVERGED counts as OK); statuses, when
+ * not NULL, receives every member's own status (read once, after the last step). Failure text:
+ * skt_last_error(NULL). */
+skt_status skt_ensemble_step(skt_ensemble* ens, const float* dt, float dt0, const float* speed, int nsteps, int* statuses);
+
 /* Field readback: the per-field copies of editor::GPUSetEnv (Game/editor.cpp:226-260).
  * dir selects the wind component for SKT_WIND. n must equal nx*ny*nz. Synchronous. */
 skt_status skt_read_field(skt_env* env, int param, int dir, float* host_dst, size_t n);
@@ -415,7 +432,7 @@ skt_status skt_view_volume(skt_env* env, int sky_param, int ground_param, const 
 skt_status skt_export_bricks(skt_env* env, int param, int dir, float background, float threshold, int half,
                              uint32_t* coords, void* values, size_t capacity, size_t* count);
 
-/* Text of the last error on env (or, when env is NULL, of the last skt_create,
+/* Text of the last error on env (or, when env is NULL, of the last skt_create, skt_ensemble_*,
  * skt_diffuse_noalloc or skt_sounding_* failure on this thread). */
 const char* skt_last_error(const skt_env* env);
 

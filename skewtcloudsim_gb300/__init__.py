@@ -5,10 +5,10 @@ include/skewt.h). This package holds the host-side mirror of the reference's env
 (``Environment``), the synthetic sounding generator, the radiosonde readers (``radiosonde``)
 and the build recipe.
 """
-from .environment import (Environment, SolverConfig, step_ensemble, Parameter, Direction, Ground, Column, Status,
+from .environment import (Environment, Ensemble, SolverConfig, step_ensemble, Parameter, Direction, Ground, Column, Status,
                           SktError, FIELDS, GROUND_FIELDS, COLUMNS, DIAG_BUOYANCY, RATE_NAMES)
 from . import sounding
 from . import radiosonde
 
-__all__ = ["radiosonde", "step_ensemble", "Environment", "SolverConfig", "Parameter", "Direction", "Ground", "Column", "Status", "SktError",
+__all__ = ["radiosonde", "step_ensemble", "Ensemble", "Environment", "SolverConfig", "Parameter", "Direction", "Ground", "Column", "Status", "SktError",
            "FIELDS", "GROUND_FIELDS", "COLUMNS", "DIAG_BUOYANCY", "RATE_NAMES", "sounding"]

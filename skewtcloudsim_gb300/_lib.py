@@ -109,6 +109,10 @@ SIGNATURES.update({
     "skt_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "skt_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "skt_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(Tuning)]),
+    "skt_ensemble_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "skt_ensemble_destroy": (None, [ctypes.c_void_p]),
+    "skt_ensemble_step": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_float, c_float_p, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int)]),
 })
 
 _lib = None

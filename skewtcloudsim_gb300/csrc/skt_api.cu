@@ -196,22 +196,23 @@ void drop_graph(Env& e) {
     if (e.graph) cudaGraphDestroy(e.graph);
     e.graph_exec = nullptr;
     e.graph = nullptr;
-    e.irr_node = nullptr;
+    e.book = GraphBook{};
 }
 
-// Captures one step (as queue_step queues it) into e.graph_exec.
-skt_status capture_step(Env& e, float dt, float speed) {
-    drop_graph(e);
+skt_status ensure_side_streams(Env& e) {
     for (int i = 0; i < 4; ++i)
         if (!e.side[i] && cudaStreamCreateWithFlags(&e.side[i], cudaStreamNonBlocking) != cudaSuccess)
             return fail(&e, SKT_CUDA_ERROR, "graph: side stream creation failed");
-    e.graph_fail = false;
-    e.graph_err.clear();
+    return SKT_OK;
+}
+
+// Queues one step of e into the capture that e.stream takes part in (its own, or an ensemble's),
+// with the irradiance node first, and fills `book`.
+void capture_into(Env& e, float dt, float speed, GraphBook& book) {
     e.graph_loops = 0;
     e.body_acc = 0;
     e.graph_depth = 0;
     const long long l0 = e.launches;
-    GCHECK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeRelaxed));
     e.capturing = true;
     e.irr_dev = &e.sc->irr;
     k_set_irr<<<1, 1, 0, e.stream>>>(e.irr_dev, 0.0f);
@@ -221,19 +222,39 @@ skt_status capture_step(Env& e, float dt, float speed) {
         const cudaGraphNode_t* deps = nullptr;
         size_t nd = 0;
         GCHECK(cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
-        e.irr_node = (nd == 1 && deps) ? deps[0] : nullptr;
+        book.irr_node = (nd == 1 && deps) ? deps[0] : nullptr;
     }
     queue_step(e, dt, speed, 0.0f);
-    cudaGraph_t graph = nullptr;
-    GCHECK(cudaStreamEndCapture(e.stream, &graph));
     e.capturing = false;
     const long long captured = e.launches - l0;
     e.launches = l0;
-    e.graph = graph;
-    if (!e.graph_fail && !e.irr_node) {
+    book.statics = captured - e.body_acc;
+    book.loops = e.graph_loops;
+    for (int l = 0; l < e.graph_loops; ++l) book.body[l] = e.loop_body[l];
+    if (!e.graph_fail && !book.irr_node) {
         e.graph_fail = true;
         e.graph_err = "graph: the irradiance node was not found";
     }
+}
+
+// the device's trip counters as they stand (a captured step's loops count on from there)
+void read_trips(Env& e) {
+    cudaMemcpyAsync(e.trips_seen, e.sc->trips, sizeof(e.trips_seen), cudaMemcpyDeviceToHost, e.stream);
+    cudaStreamSynchronize(e.stream);
+}
+
+// Captures one step (as queue_step queues it) into e.graph_exec.
+skt_status capture_step(Env& e, float dt, float speed) {
+    drop_graph(e);
+    if (ensure_side_streams(e) != SKT_OK) return SKT_CUDA_ERROR;
+    e.graph_fail = false;
+    e.graph_err.clear();
+    GCHECK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeRelaxed));
+    GraphBook book;
+    capture_into(e, dt, speed, book);
+    cudaGraph_t graph = nullptr;
+    GCHECK(cudaStreamEndCapture(e.stream, &graph));
+    e.graph = graph;
     if (!e.graph_fail) GCHECK(cudaGraphInstantiate(&e.graph_exec, graph, 0));
     if (e.graph_fail) {
         cudaGetLastError();
@@ -241,46 +262,41 @@ skt_status capture_step(Env& e, float dt, float speed) {
         drop_graph(e);
         return fail(&e, SKT_CUDA_ERROR, m);
     }
-    e.graph_static = captured - e.body_acc;
+    e.book = book;
     e.gkey = graph_key(e, dt, speed);
-    // the trip counters keep counting from where they stand
-    cudaMemcpyAsync(e.trips_seen, e.sc->trips, sizeof(e.trips_seen), cudaMemcpyDeviceToHost, e.stream);
-    cudaStreamSynchronize(e.stream);
+    read_trips(e);
     return cuda_check(e, "graph capture");
 }
 
-// nsteps launches of the captured step; the host reads the solver scalars once at the end
-skt_status step_graph(Env& e, float dt, float speed, int nsteps) {
-    if (!e.graph_exec || !same_key(e.gkey, graph_key(e, dt, speed))) {
-        const skt_status st = capture_step(e, dt, speed);
-        if (st != SKT_OK) return st;
+// Before a launch of a captured step: the ground block after an edit (queued on `before`, which the
+// launch follows) and this step's irradiance into the step's irradiance node.
+skt_status prepare_launch(Env& e, cudaGraphExec_t exec, const GraphBook& book, cudaStream_t before) {
+    if (e.ground_changed) {
+        cudaStream_t own = e.stream;
+        e.stream = before;
+        launch_editor_block(e);
+        e.stream = own;
     }
-    if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
-    cudaEventRecord(e.ev0, e.stream);
-    for (int i = 0; i < nsteps; ++i) {
-        if (e.ground_changed) launch_editor_block(e);  // after a ground edit, outside the graph
-        e.ground_changed = 0;
-        float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
-        cudaKernelNodeParams kp{};
-        void* args[2] = {&e.irr_dev, &irr};
-        kp.func = (void*)k_set_irr;
-        kp.gridDim = dim3(1);
-        kp.blockDim = dim3(1);
-        kp.kernelParams = args;
-        if (cudaGraphExecKernelNodeSetParams(e.graph_exec, e.irr_node, &kp) != cudaSuccess) return cuda_check(e, "graph irradiance update");
-        if (cudaGraphLaunch(e.graph_exec, e.stream) != cudaSuccess) return cuda_check(e, "graph launch");
-        advance_clock(e, dt, speed);
-    }
-    cudaEventRecord(e.ev1, e.stream);
-    cudaEventSynchronize(e.ev1);
-    cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
-    const skt_status st = cuda_check(e, "graph step");
-    if (st != SKT_OK) return st;
+    e.ground_changed = 0;
+    float irr = irradiance(e.sim_time, e.day, e.longitude, e.sun);
+    cudaKernelNodeParams kp{};
+    void* args[2] = {&e.irr_dev, &irr};
+    kp.func = (void*)k_set_irr;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = args;
+    if (cudaGraphExecKernelNodeSetParams(exec, book.irr_node, &kp) != cudaSuccess) return cuda_check(e, "graph irradiance update");
+    return SKT_OK;
+}
+
+// After launches of a captured step (the stream synchronised): the solver scalars, the stats and
+// the kernel count from the trip counters.
+void finish_graph_steps(Env& e, const GraphBook& book, int nsteps) {
     fetch_scalars(e);
     const Scalars& h = *e.host_sc;
-    long long ran = e.graph_static * nsteps;
-    for (int l = 0; l < e.graph_loops; ++l) {
-        ran += (long long)(h.trips[l] - e.trips_seen[l]) * e.loop_body[l];
+    long long ran = book.statics * nsteps;
+    for (int l = 0; l < book.loops; ++l) {
+        ran += (long long)(h.trips[l] - e.trips_seen[l]) * book.body[l];
         e.trips_seen[l] = h.trips[l];
     }
     e.launches += ran;
@@ -295,6 +311,43 @@ skt_status step_graph(Env& e, float dt, float speed, int nsteps) {
         e.last_residual = h.residual;
         e.last_converged = h.converged == 1;
     }
+}
+
+// the status a graph step left on the device, turned into the call's result (and cleared)
+skt_status graph_status(Env& e) {
+    const int dev_status = e.host_sc->status;
+    if (dev_status != 0) {
+        cudaMemsetAsync(&e.sc->status, 0, sizeof(int), e.stream);
+        cudaStreamSynchronize(e.stream);
+        e.host_sc->status = 0;
+        return fail(&e, skt_status(dev_status),
+                    dev_status == SKT_TIMEOUT ? "a kernel's wait for its streamed data ran out (the state is not valid)"
+                                              : "a step of this call met a NaN or Inf (in the wind or in a pressure-solver "
+                                                "reduction: a non-finite field value or a zero-density cell); the state is not valid");
+    }
+    return e.last_converged ? SKT_OK : SKT_NOT_CONVERGED;
+}
+
+// nsteps launches of the captured step; the host reads the solver scalars once at the end
+skt_status step_graph(Env& e, float dt, float speed, int nsteps) {
+    if (!e.graph_exec || !same_key(e.gkey, graph_key(e, dt, speed))) {
+        const skt_status st = capture_step(e, dt, speed);
+        if (st != SKT_OK) return st;
+    }
+    if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
+    cudaEventRecord(e.ev0, e.stream);
+    for (int i = 0; i < nsteps; ++i) {
+        const skt_status ps = prepare_launch(e, e.graph_exec, e.book, e.stream);
+        if (ps != SKT_OK) return ps;
+        if (cudaGraphLaunch(e.graph_exec, e.stream) != cudaSuccess) return cuda_check(e, "graph launch");
+        advance_clock(e, dt, speed);
+    }
+    cudaEventRecord(e.ev1, e.stream);
+    cudaEventSynchronize(e.ev1);
+    cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
+    const skt_status st = cuda_check(e, "graph step");
+    if (st != SKT_OK) return st;
+    finish_graph_steps(e, e.book, nsteps);
     return SKT_OK;
 }
 
@@ -636,17 +689,7 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
         // graph mode: the status is read once after the nsteps launches
         const skt_status gs = step_graph(e, dt, speed, nsteps);
         if (gs != SKT_OK) return gs;
-        const int dev_status = e.host_sc->status;
-        if (dev_status != 0) {
-            cudaMemsetAsync(&e.sc->status, 0, sizeof(int), e.stream);
-            cudaStreamSynchronize(e.stream);
-            e.host_sc->status = 0;
-            return fail(&e, skt_status(dev_status),
-                        dev_status == SKT_TIMEOUT ? "a kernel's wait for its streamed data ran out (the state is not valid)"
-                                                  : "a step of this call met a NaN or Inf (in the wind or in a pressure-solver "
-                                                    "reduction: a non-finite field value or a zero-density cell); the state is not valid");
-        }
-        return e.last_converged ? SKT_OK : SKT_NOT_CONVERGED;
+        return graph_status(e);
     }
     skt_status worst = SKT_OK;
     if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
@@ -681,6 +724,166 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
                           "the state is not valid");
     }
     return worst;
+}
+
+}  // extern "C"
+
+// An ensemble captured as one CUDA graph: every member's whole step is an independent branch of
+// the graph (forked from and joined to the ensemble's stream), so one graph launch advances all
+// members and the GPU runs their kernels side by side; no host thread per member and no host
+// synchronisation inside a step.
+struct skt_ensemble {
+    std::vector<skt_env*> members;
+    std::vector<GraphBook> books;
+    std::vector<Env::GraphKey> keys;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    float last_ms = 0.0f;
+};
+
+namespace {
+void drop_ensemble_graph(skt_ensemble* s) {
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->exec = nullptr;
+    s->graph = nullptr;
+}
+
+skt_status capture_ensemble(skt_ensemble* s, const std::vector<float>& dts, const std::vector<float>& sps) {
+    drop_ensemble_graph(s);
+    const int n = int(s->members.size());
+    for (int i = 0; i < n; ++i) {
+        Env& e = s->members[i]->e;
+        if (ensure_side_streams(e) != SKT_OK) return fail(nullptr, SKT_CUDA_ERROR, "ensemble: member " + std::to_string(i) + ": " + e.err);
+        e.graph_fail = false;
+        e.graph_err.clear();
+    }
+    if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess || cudaEventRecord(s->fork, s->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, SKT_CUDA_ERROR, "ensemble: capture could not begin");
+    }
+    for (int i = 0; i < n; ++i) {
+        Env& e = s->members[i]->e;
+        cudaStreamWaitEvent(e.stream, s->fork, 0);
+        capture_into(e, dts[i], sps[i], s->books[i]);
+        cudaEventRecord(s->joins[i], e.stream);
+        cudaStreamWaitEvent(s->stream, s->joins[i], 0);
+        s->keys[i] = graph_key(e, dts[i], sps[i]);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t end = cudaStreamEndCapture(s->stream, &graph);
+    s->graph = graph;
+    std::string err;
+    for (int i = 0; i < n && err.empty(); ++i)
+        if (s->members[i]->e.graph_fail) err = "ensemble: member " + std::to_string(i) + ": " + s->members[i]->e.graph_err;
+    if (err.empty() && end != cudaSuccess) err = std::string("ensemble: capture: ") + cudaGetErrorString(end);
+    if (err.empty() && cudaGraphInstantiate(&s->exec, graph, 0) != cudaSuccess) err = "ensemble: graph instantiation failed";
+    if (!err.empty()) {
+        cudaGetLastError();
+        drop_ensemble_graph(s);
+        return fail(nullptr, SKT_CUDA_ERROR, err);
+    }
+    for (int i = 0; i < n; ++i) read_trips(s->members[i]->e);
+    return SKT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+skt_status skt_ensemble_create(skt_env* const* envs, int n, skt_ensemble** out) {
+    if (!envs || n < 1 || !out) return fail(nullptr, SKT_INVALID_ARG, "invalid ensemble arguments");
+    *out = nullptr;
+    int device = -1;
+    for (int i = 0; i < n; ++i) {
+        if (!envs[i]) return fail(nullptr, SKT_INVALID_ARG, "null member");
+        for (int j = 0; j < i; ++j)
+            if (envs[j] == envs[i]) return fail(nullptr, SKT_INVALID_ARG, "a member appears twice");
+        if (device >= 0 && envs[i]->e.device != device) return fail(nullptr, SKT_INVALID_ARG, "members on different devices");
+        device = envs[i]->e.device;
+    }
+    skt_ensemble* s = new (std::nothrow) skt_ensemble();
+    if (!s) return fail(nullptr, SKT_OUT_OF_MEMORY, "host allocation failed");
+    s->members.assign(envs, envs + n);
+    s->books.resize(n);
+    s->keys.resize(n);
+    s->joins.resize(n, nullptr);
+    bool ok = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) == cudaSuccess && cudaEventCreate(&s->ev0) == cudaSuccess &&
+              cudaEventCreate(&s->ev1) == cudaSuccess;
+    for (int i = 0; ok && i < n; ++i) ok = cudaEventCreateWithFlags(&s->joins[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        skt_ensemble_destroy(s);
+        return fail(nullptr, SKT_CUDA_ERROR, "ensemble: stream or event creation failed");
+    }
+    *out = s;
+    return SKT_OK;
+}
+
+void skt_ensemble_destroy(skt_ensemble* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    drop_ensemble_graph(s);
+    for (cudaEvent_t ev : s->joins)
+        if (ev) cudaEventDestroy(ev);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+skt_status skt_ensemble_step(skt_ensemble* s, const float* dt, float dt0, const float* speed, int nsteps, int* statuses) {
+    if (!s || nsteps < 0) return fail(nullptr, SKT_INVALID_ARG, "invalid ensemble step arguments");
+    const int n = int(s->members.size());
+    std::vector<float> dts(n), sps(n);
+    for (int i = 0; i < n; ++i) {
+        Env& e = s->members[i]->e;
+        if (!e.initialized) return fail(nullptr, SKT_NOT_INITIALIZED, "member " + std::to_string(i) + ": skt_init has not run");
+        dts[i] = dt ? dt[i] : dt0;
+        sps[i] = speed ? speed[i] : 1.0f;
+        if (!(dts[i] > 0.0f) || !(sps[i] > 0.0f)) return fail(nullptr, SKT_INVALID_ARG, "dt and speed must be > 0");
+    }
+    if (nsteps == 0) return SKT_OK;
+    bool stale = !s->exec;
+    for (int i = 0; i < n && !stale; ++i) stale = !same_key(s->keys[i], graph_key(s->members[i]->e, dts[i], sps[i]));
+    if (stale) {
+        const skt_status st = capture_ensemble(s, dts, sps);
+        if (st != SKT_OK) return st;
+    }
+    cudaEventRecord(s->ev0, s->stream);
+    for (int k = 0; k < nsteps; ++k) {
+        for (int i = 0; i < n; ++i) {
+            const skt_status ps = prepare_launch(s->members[i]->e, s->exec, s->books[i], s->stream);
+            if (ps != SKT_OK) return fail(nullptr, ps, "member " + std::to_string(i) + ": " + s->members[i]->e.err);
+        }
+        if (cudaGraphLaunch(s->exec, s->stream) != cudaSuccess) {
+            const std::string m = cudaGetErrorString(cudaGetLastError());
+            return fail(nullptr, SKT_CUDA_ERROR, "ensemble: graph launch: " + m);
+        }
+        for (int i = 0; i < n; ++i) advance_clock(s->members[i]->e, dts[i], sps[i]);
+    }
+    cudaEventRecord(s->ev1, s->stream);
+    cudaEventSynchronize(s->ev1);
+    cudaEventElapsedTime(&s->last_ms, s->ev0, s->ev1);
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(nullptr, SKT_CUDA_ERROR, std::string("ensemble step: ") + cudaGetErrorString(err));
+    skt_status first = SKT_OK;
+    for (int i = 0; i < n; ++i) {
+        Env& e = s->members[i]->e;
+        finish_graph_steps(e, s->books[i], nsteps);
+        e.last_gpu_ms = s->last_ms;
+        const skt_status st = graph_status(e);
+        if (statuses) statuses[i] = st;
+        if (st != SKT_OK && st != SKT_NOT_CONVERGED && first == SKT_OK) {
+            first = st;
+            fail(nullptr, st, "member " + std::to_string(i) + ": " + e.err);
+        }
+    }
+    return first;
 }
 
 skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float dt0, const float* speed, int nsteps,

@@ -142,6 +142,16 @@ struct Tuning {
     int ppmy_bps = 32;       // k_ppm4y: blocks per SM (y-run length)
 };
 
+// What a captured step needs at launch and afterwards: the irradiance node to update, and the
+// kernel counts (outside the loops, and per trip of each loop) to count the launches from the
+// device's trip counters.
+struct GraphBook {
+    cudaGraphNode_t irr_node = nullptr;
+    long long statics = 0;
+    int loops = 0;
+    long long body[kMaxGraphLoops] = {0};
+};
+
 struct Env {
     Grid g{};
     SolverCfg cfg{};
@@ -193,16 +203,15 @@ struct Env {
     int graph_depth = 0;
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;
-    cudaGraphNode_t irr_node = nullptr;  // the node that stores the step's irradiance (updated per launch)
     float* irr_dev = nullptr;            // the irradiance the ground kernel reads in graph mode
     struct GraphKey {
         float dt, speed;
         int flat, rates_on, rate_lo[3], rate_hi[3], diag_flags;
         Tuning tune;
     } gkey{};
-    long long graph_static = 0;          // kernels of one launch outside the loop bodies
-    int graph_loops = 0;                 // loops captured
-    long long loop_body[kMaxGraphLoops] = {0};  // kernels of one trip of each loop body (nested bodies excluded)
+    GraphBook book;                      // the bookkeeping of the environment's own captured step
+    int graph_loops = 0;                 // capture in progress: loops captured so far
+    long long loop_body[kMaxGraphLoops] = {0};  // capture in progress: kernels of one trip of each loop body
     unsigned int trips_seen[kMaxGraphLoops] = {0};
     long long body_acc = 0;              // capture bookkeeping: kernels inside loop bodies at the current level
     bool graph_fail = false;             // a capture call failed

@@ -384,3 +384,41 @@ def step_ensemble(envs, dt, speed=1.0, nsteps: int = 1, threads: int = 0):
     if rc != 0:
         raise SktError(rc, L.skt_last_error(None).decode())
     return [Status(v) for v in st]
+
+
+class Ensemble:
+    """skt_ensemble_*: members advanced together by one CUDA graph launch per step (every member's
+    whole step an independent branch of the graph). The members must stay open while it exists."""
+
+    def __init__(self, envs):
+        self._L = _lib.load()
+        self.envs = list(envs)
+        n = len(self.envs)
+        hs = (ctypes.c_void_p * n)(*[e._h.value if hasattr(e._h, "value") else e._h for e in self.envs])
+        self._h = ctypes.c_void_p()
+        rc = self._L.skt_ensemble_create(hs, n, ctypes.byref(self._h))
+        if rc != 0:
+            raise SktError(rc, self._L.skt_last_error(None).decode())
+
+    def step(self, dt, speed=1.0, nsteps: int = 1):
+        """Advances every member; returns their statuses, raises on the first failing member."""
+        n = len(self.envs)
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float32), (n,)))
+        sps = np.ascontiguousarray(np.broadcast_to(np.asarray(speed, np.float32), (n,)))
+        st = (ctypes.c_int * n)()
+        rc = self._L.skt_ensemble_step(self._h, _fp(dts), 0.0, _fp(sps), int(nsteps), st)
+        if rc not in (0, int(Status.NOT_CONVERGED)):
+            raise SktError(rc, self._L.skt_last_error(None).decode())
+        return [Status(v) for v in st]
+
+    def close(self):
+        if self._h:
+            self._L.skt_ensemble_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -62,3 +62,35 @@ def test_ensemble_errors(gpu_lib):
     with pytest.raises(SktError, match="member 0"):
         step_ensemble([env], 0.5)
     env.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_ensemble_equals_members_stepped_alone(gpu_lib, precision):
+    """skt_ensemble_step (one graph launch per step for all members) against the members stepped
+    one by one, stream-ordered: the same bits, the same substep and iteration counts; the
+    ensemble steps again after one member was stepped alone (its trip counters stay consistent)."""
+    from skewtcloudsim_gb300 import Ensemble
+    a = _members(6, precision)
+    b = _members(6, precision)
+    ens = Ensemble([m[0] for m in a])
+    ens.step([m[2] for m in a], 1.0, nsteps=2)
+    for env, _, dt, speed in b:
+        env.update_gpu(dt, speed, nsteps=2)
+    a[0][0].update_gpu(a[0][2], 1.0)  # one member alone, between ensemble steps
+    b[0][0].update_gpu(b[0][2], 1.0)
+    st = ens.step([m[2] for m in a], 1.0)
+    for env, _, dt, speed in b:
+        env.update_gpu(dt, speed)
+    assert len(st) == 6
+    for (ea, *_), (eb, *_) in zip(a, b):
+        m = ea.sky_mask()
+        for k in SKY:
+            assert np.isfinite(ea.read(k)[m]).all(), k
+            np.testing.assert_array_equal(ea.read(k).view(np.uint32), eb.read(k).view(np.uint32), err_msg=k)
+        sa, sb = ea.stats(), eb.stats()
+        assert sa["nsub"] == sb["nsub"] and sa["pcg_iters"] == sb["pcg_iters"], (sa, sb)
+        assert sa["kernel_launches"] > 0
+    ens.close()
+    for m in a + b:
+        m[0].close()
+
