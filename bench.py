@@ -274,12 +274,29 @@ def survey_step_bytes(mode, pcg_iters, outer):
     return 2558.0 + 52.0 * pcg_iters
 
 
+TUNING_CACHE = os.path.join(ROOT, "skewtcloudsim_gb300", "_build", "tuning.json")
+
+
+def apply_tuning(args, env):
+    """The launch shapes of the run: --tuning's values, else the autotuner's (cached per GPU and
+    grid in the build folder, measured on the first run), else the defaults."""
+    if args.tuning:
+        kv = dict(item.split("=") for item in args.tuning.split(","))
+        env.set_tuning(**{k: int(v) for k, v in kv.items()})
+        return dict(env.get_tuning(), source="--tuning")
+    if args.no_autotune:
+        return dict(env.get_tuning(), source="defaults")
+    t = env.autotune(TUNING_CACHE)
+    return dict(env.get_tuning(), source="autotune cache" if t["from_cache"] else "autotune (measured this run)")
+
+
 def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
     from skewtcloudsim_gb300 import Environment
     cfg = mode_config(args, mode)
     sem = cfg.semantics
     env = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
     env.init_from(init)
+    tuning = apply_tuning(args, env)
     for _ in range(args.warmup):
         env.update_gpu(dt, speed)
     env.sync()
@@ -312,6 +329,7 @@ def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
     sd = env.stats()
     env.close()
     return {"mode": mode, "semantics": "reference" if sem == 0 else "textbook", "value": value, "ms_per_step": ms_per_step,
+            "tuning": tuning,
             "launches": int(launches), "clocks": clk.summary(), "prof": prof, "pcg_iters": sd["pcg_iters"],
             "outer": sd.get("outer_iters", 0), "converged": sd["converged"], "residual": sd["pcg_residual"],
             "pcg_max_iter": cfg.pcg_max_iter}
@@ -411,6 +429,9 @@ def main():
                     help="1 = each step one launch of the captured CUDA graph (device-side loops), 0 = stream-ordered")
     ap.add_argument("--ensemble-runner", default="graph", choices=["graph", "threads"],
                     help="ensemble workloads: one graph launch per step for all members, or a host thread per member")
+    ap.add_argument("--tuning", default="",
+                    help="launch shapes to set instead of the autotuner's choice, e.g. diffuse_depth=2,diffuse_rows=8")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--shape", default=None, help="x,y,z (z vertical) override of the workload size")
@@ -478,10 +499,12 @@ def main():
         cfg = mode_config(args, head["mode"])
         env2 = Environment(init.nx, init.ny, init.nz, init.voxel, cfg)
         K = args.steps
+        tuned = {k: v for k, v in head["tuning"].items() if k != "source"}
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         env2.init(host_in["theta"][0], host_in["vel"][0], host_in["qv"][0], host_in["ground_T"][0],
                   host_in["ground_p"][0], host_in["p3d"][0], host_in["p_column"][0], init.ground_height)
+        env2.set_tuning(**tuned)
         host_outs = {k: outs[k][0] for k in names}
         for _ in range(K):
             env2.update_gpu(dt, speed)
@@ -510,7 +533,7 @@ def main():
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": args.workload, "grid_xyz": [init.nx, init.nz, init.ny], "cells": cells,
                       "dt": dt, "pcg": head["mode"], "semantics": head["semantics"],
-                      "pcg_iters_per_step": head["pcg_iters"],
+                      "pcg_iters_per_step": head["pcg_iters"], "graph": bool(args.graph), "tuning": head["tuning"],
                       "l2": (f"inputs larger than L2 ({field_mb:.0f} MB per field, L2 129 MB)" if field_mb > 129
                              else f"fields of {field_mb:.0f} MB fit in L2 (129 MB): timings include L2 reuse"),
                       "parallelism": "replicas" if world > 1 else "single"},
