@@ -78,6 +78,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, pg, device):
+    """The largest x over the ranks (the slowest rank's time); x itself with one rank. pg is the
+    torch.distributed module once its process group is up (nccl on GPUs, gloo in the CPU tests)."""
+    if not pg:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Replicas: every rank processes the same units (weak scaling), so the job's rate is all ranks'
+    units over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled during the timed region."""
 
@@ -176,6 +193,7 @@ def cpu_baseline(workload: str, sample_shape, steps: int = 1, threads: int = 0):
 
 
 CPU_SAMPLE = (128, 128, 64)  # (x, y, z), z vertical: the bounded sub-box of the CPU legs (1.05M cells)
+CPU_STEPS = 10  # steps of the headline CPU leg: about 10 s on 16 Arm cores
 
 
 def cpu_thread_sweep(workload: str, sample_shape):
@@ -315,12 +333,9 @@ def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
     st = env.stats()
     ms_total = st["gpu_ms"]
     launches = st["kernel_launches"] - l0
-    if pg:
-        t = torch.tensor([ms_total], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ms_total, pg, "cuda")
     ms_per_step = ms_total / args.steps
-    value = cells * args.steps * world / (ms_total / 1e3)
+    value = whole_job_rate(cells * args.steps, world, ms_total / 1e3)
     # ---- per-stage profile of one more step (not timed) ----------------------------------
     env.profile(True)
     env.update_gpu(dt, speed)
@@ -382,10 +397,7 @@ def run_ensemble(args, rank, world, local, pg, torch):
         torch.cuda.synchronize()
         other = (time.perf_counter() - o0) / args.steps * 1e3
         ens.close()
-    if pg:
-        t = torch.tensor([el], device="cuda")
-        pg.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
+    el = max_over_ranks(el, pg, "cuda")
     # one sequential pass for comparison: the same members stepped one after another
     torch.cuda.synchronize()
     s0 = time.perf_counter()
@@ -396,7 +408,7 @@ def run_ensemble(args, rank, world, local, pg, torch):
     for env in envs:
         env.close()
     if rank == 0:
-        value = cells * args.steps * world / el
+        value = whole_job_rate(cells * args.steps, world, el)
         print(json.dumps({
             "metric": f"members x cell-steps/s, ensemble of {n} uneven members", "value": value, "unit": "cell-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
@@ -523,7 +535,7 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        cpu = cpu_baseline(args.workload, CPU_SAMPLE, 1)
+        cpu = cpu_baseline(args.workload, CPU_SAMPLE, CPU_STEPS)
         cpu["thread_sweep"] = cpu_thread_sweep(args.workload, CPU_SAMPLE)
         cpu["host"] = {"nproc": os.cpu_count(), "cpu": host_cpu()}
 
