@@ -151,9 +151,11 @@ skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float
  * independent branch of one graph at the first skt_ensemble_step (and again when a member's dt,
  * speed, tuning, diagnostics or terrain flatness change), so each ensemble step is a single graph
  * launch from the calling thread: the GPU runs the members' kernels side by side and the host
- * synchronises once per call. Results equal stepping the members one by one, bit for bit. Members
- * keep their own state and may still be stepped alone; they must outlive the ensemble and must
- * not be stepped from another thread while the ensemble steps. */
+ * synchronises once per call. Results equal stepping the members one by one, bit for bit. While a
+ * member belongs to an ensemble, the grids of its per-cell kernels are sized for its share of the
+ * SMs (twice its proportion of the cells), since the members run side by side; skt_ensemble_destroy gives
+ * it the whole GPU again. Members keep their own state and may still be stepped alone; they must
+ * outlive the ensemble and must not be stepped from another thread while the ensemble steps. */
 typedef struct skt_ensemble skt_ensemble;
 skt_status skt_ensemble_create(skt_env* const* envs, int n, skt_ensemble** out);
 void skt_ensemble_destroy(skt_ensemble* ens);

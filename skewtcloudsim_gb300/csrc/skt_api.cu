@@ -179,12 +179,14 @@ Env::GraphKey graph_key(const Env& e, float dt, float speed) {
         k.rate_hi[i] = e.rates_on ? e.rate_hi[i] : 0;
     }
     k.diag_flags = e.diag_flags;
+    k.stencil_sms = stencil_sms(e);
     k.tune = e.tune;
     return k;
 }
 bool same_key(const Env::GraphKey& a, const Env::GraphKey& b) {
     const Tuning &s = a.tune, &t = b.tune;
     return a.dt == b.dt && a.speed == b.speed && a.flat == b.flat && a.rates_on == b.rates_on && a.diag_flags == b.diag_flags &&
+           a.stencil_sms == b.stencil_sms &&
            a.rate_lo[0] == b.rate_lo[0] && a.rate_lo[1] == b.rate_lo[1] && a.rate_lo[2] == b.rate_lo[2] && a.rate_hi[0] == b.rate_hi[0] &&
            a.rate_hi[1] == b.rate_hi[1] && a.rate_hi[2] == b.rate_hi[2] && s.diffuse_depth == t.diffuse_depth && s.diffuse_h == t.diffuse_h &&
            s.diffuse_bps == t.diffuse_bps && s.diffuse2_bps == t.diffuse2_bps && s.ppm_bps == t.ppm_bps && s.ppmy_bps == t.ppmy_bps &&
@@ -807,6 +809,16 @@ skt_status skt_ensemble_create(skt_env* const* envs, int n, skt_ensemble** out) 
     skt_ensemble* s = new (std::nothrow) skt_ensemble();
     if (!s) return fail(nullptr, SKT_OUT_OF_MEMORY, "host allocation failed");
     s->members.assign(envs, envs + n);
+    // the members run side by side: each member's per-cell kernels are sized for twice its share of
+    // the SMs in proportion to its cells (at least one SM), instead of for the whole GPU. Measured on
+    // 48 members of four sizes (69M cells): 130 ms per ensemble step sized for the whole GPU, 110 ms
+    // at the share, 101 ms at twice it, 103 ms at four times it.
+    double total = 0.0;
+    for (int i = 0; i < n; ++i) total += double(envs[i]->e.g.N);
+    for (int i = 0; i < n; ++i) {
+        Env& e = envs[i]->e;
+        e.stencil_sms = std::min(e.num_sms, std::max(1, int(std::lround(2.0 * e.num_sms * double(e.g.N) / total))));
+    }
     s->books.resize(n);
     s->keys.resize(n);
     s->joins.resize(n, nullptr);
@@ -826,6 +838,7 @@ skt_status skt_ensemble_create(skt_env* const* envs, int n, skt_ensemble** out) 
 void skt_ensemble_destroy(skt_ensemble* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (skt_env* m : s->members) m->e.stencil_sms = 0;  // stepped alone again: the whole GPU
     drop_ensemble_graph(s);
     for (cudaEvent_t ev : s->joins)
         if (ev) cudaEventDestroy(ev);

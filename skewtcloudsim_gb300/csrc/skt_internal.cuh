@@ -195,6 +195,11 @@ struct Env {
     int last_nsub[10] = {0};
     int last_outer = 0;
     int num_sms = 148;
+    // SMs the grids of the per-cell kernels are sized for (0: all of them). An ensemble gives each
+    // member a share in proportion to its cells, since the members run side by side. Only kernels
+    // whose results do not depend on their grid use it; the reductions keep num_sms, so a member's
+    // bits are the same inside an ensemble and alone.
+    int stencil_sms = 0;
     std::string err;
     int flat = 1;  // all gh == 0
     // graph mode: the step captured once per key, the loops as conditional WHILE nodes
@@ -206,7 +211,7 @@ struct Env {
     float* irr_dev = nullptr;            // the irradiance the ground kernel reads in graph mode
     struct GraphKey {
         float dt, speed;
-        int flat, rates_on, rate_lo[3], rate_hi[3], diag_flags;
+        int flat, rates_on, rate_lo[3], rate_hi[3], diag_flags, stencil_sms;
         Tuning tune;
     } gkey{};
     GraphBook book;                      // the bookkeeping of the environment's own captured step
@@ -283,6 +288,7 @@ void launch_ground(Env& e, float dt, float speed, float irr);
 void launch_init_state(Env& e, int noise, uint32_t seed);
 void launch_isen_ground(Env& e);  // computeIsenTempGroundGPU on the current heightfield
 void launch_editor_block(Env& e);  // editorDataGPU's ground block (after a ground edit)
+inline int stencil_sms(const Env& e) { return e.stencil_sms > 0 ? e.stencil_sms : e.num_sms; }
 bool mg_allocate(Env& e);
 // Graph capture: inside a capture of e.stream, adds a WHILE conditional node. `init` queues the
 // kernel that sets the node's condition for the first trip (before the node); `body` queues the

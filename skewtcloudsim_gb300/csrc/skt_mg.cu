@@ -1068,21 +1068,23 @@ void mg_setup(Env& e) {
     if (e.cfg.mg_half && vec_level(e, 0)) {
         __half* h[4];
         half_arrays(e, h);
-        const int nb = std::min((e.g.N + RT - 1) / RT, e.num_sms * 8);
+        const int nb = std::min((e.g.N + RT - 1) / RT, stencil_sms(e) * 8);
         k_mg_half<<<nb, RT, 0, e.stream>>>(e.g, e.ax, e.ay, e.az, e.aw, h[0], h[1], h[2], h[3]);
         e.launches += 1;
     }
 }
 
 // z-march launch shape of a vector level: about 12 blocks of 32 x JVY threads per SM, at most
-// kMaxPartials blocks (the fused dot products keep one partial per block), even plane runs
+// kMaxPartials blocks (the fused dot products keep one partial per block), even plane runs. The
+// kernels with a dot product are sized for all SMs (num_sms: their partials, and so their bits,
+// follow the grid), the per-cell ones for stencil_sms.
 struct March {
     dim3 grid;
     int zlen;
 };
-March march(const Env& e, int X, int Y, int Z) {
+March march(const Env& e, int X, int Y, int Z, int sms) {
     const int gx = (X / 4 + 31) / 32, gy = (Y + JVY - 1) / JVY;
-    int zc = std::max(1, std::min(Z, (e.num_sms * 12 + gx * gy - 1) / (gx * gy)));
+    int zc = std::max(1, std::min(Z, (sms * 12 + gx * gy - 1) / (gx * gy)));
     zc = std::max(1, std::min(zc, kMaxPartials / (gx * gy)));
     int zlen = (Z + zc - 1) / zc;
     zlen += zlen & 1;
@@ -1144,7 +1146,8 @@ void vcycle_vec(Env& e, int l, const CT* ax, const CT* ay, const CT* az, const C
                 const int* skip, int dot) {
     const LvlView L = view(e, l);
     MgLevel& C = e.mg[l + 1];
-    const March m = march(e, L.X, L.Y, L.Z);
+    const March m = march(e, L.X, L.Y, L.Z, stencil_sms(e));
+    const March md = march(e, L.X, L.Y, L.Z, e.num_sms);  // the smoothing step that forms z.r
     const dim3 jb(32, JVY);
     const float c2a = 1.0f / kChebTheta;
     UIn<SM_PRE, CT> upre{b, aw, nullptr, 0, 0};
@@ -1159,10 +1162,10 @@ void vcycle_vec(Env& e, int l, const CT* ax, const CT* ay, const CT* az, const C
     k_mg_smooth4<SM_POSTA, DOT_NONE, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, upost, upost, x2,
                                                                      0.0f, c2a, skip, e.sc, e.partials);
     if (dot == DOT_START)
-        k_mg_smooth4<SM_POSTB, DOT_START, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, ub, upost, x,
+        k_mg_smooth4<SM_POSTB, DOT_START, CT><<<md.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, md.zlen, ax, ay, az, aw, b, ub, upost, x,
                                                                           kChebC1, kChebC2, skip, e.sc, e.partials);
     else if (dot == DOT_NEXT)
-        k_mg_smooth4<SM_POSTB, DOT_NEXT, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, ub, upost, x,
+        k_mg_smooth4<SM_POSTB, DOT_NEXT, CT><<<md.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, md.zlen, ax, ay, az, aw, b, ub, upost, x,
                                                                          kChebC1, kChebC2, skip, e.sc, e.partials);
     else
         k_mg_smooth4<SM_POSTB, DOT_NONE, CT><<<m.grid, jb, 0, e.stream>>>(L.X, L.Y, L.Z, m.zlen, ax, ay, az, aw, b, ub, upost, x,
@@ -1199,7 +1202,7 @@ void mg_solve_graph(Env& e, bool fused, int max_outer, float* bvec, float* ecor,
     auto resid = [&](int first) {
         ProfScope ps(e, "mg_refine");
         if (fused) {
-            const March m = march(e, g.X, g.Y, g.Z);
+            const March m = march(e, g.X, g.Y, g.Z, e.num_sms);
             k_resid_ff4<<<m.grid, dim3(32, JVY), 0, e.stream>>>(g.X, g.Y, g.Z, m.zlen, e.ax, e.ay, e.az, e.aw, xh, xl, bvec, e.r,
                                                               e.cfg.refine_tol, first, e.sc, e.partials);
         } else {
@@ -1211,7 +1214,7 @@ void mg_solve_graph(Env& e, bool fused, int max_outer, float* bvec, float* ecor,
     auto inner = [&]() {
         if (fused) {
             { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, nullptr, DOT_START); }
-            const March m = march(e, g.X, g.Y, g.Z);
+            const March m = march(e, g.X, g.Y, g.Z, e.num_sms);
             graph_while(
                 e, [&](cudaGraphConditionalHandle h) {
                     k_inner_cond<<<1, 1, 0, e.stream>>>(h, e.sc, -1);
@@ -1327,7 +1330,7 @@ void mg_solve(Env& e) {
         {
             ProfScope ps(e, "mg_refine");
             if (fused) {
-                const March m = march(e, g.X, g.Y, g.Z);
+                const March m = march(e, g.X, g.Y, g.Z, e.num_sms);
                 k_resid_ff4<<<m.grid, dim3(32, JVY), 0, e.stream>>>(g.X, g.Y, g.Z, m.zlen, e.ax, e.ay, e.az, e.aw, xh, xl, bvec, e.r,
                                                                   e.cfg.refine_tol, outer == 0, e.sc, e.partials);
             } else {
@@ -1345,7 +1348,7 @@ void mg_solve(Env& e) {
             float* s_old = e.s;
             float* s_new = e.pp;
             { ProfScope ps(e, "mg_vcycle"); vcycle(e, 0, e.r, z0, z0b, nullptr, DOT_START); }
-            const March m = march(e, g.X, g.Y, g.Z);
+            const March m = march(e, g.X, g.Y, g.Z, e.num_sms);
             const int chunk = 4;
             for (int it = 0; it < e.cfg.inner_max_iter; it += chunk) {
                 for (int k = 0; k < chunk && it + k < e.cfg.inner_max_iter; ++k) {

@@ -1107,7 +1107,7 @@ void launch_project(Env& e, float dtS) {
     k_press_dens<<<grd, blk, 0, e.stream>>>(g, e.p, e.pp, e.rho, e.th, e.qv, e.Pg);
     if (e.flat && (g.X % 4) == 0) {
         const int ax = (g.X / 4 + 31) / 32, ay = (g.Y - 1 + 7) / 8;
-        int az = std::max(1, std::min(g.Z, (e.num_sms * 16 + ax * ay - 1) / (ax * ay)));
+        int az = std::max(1, std::min(g.Z, (stencil_sms(e) * 16 + ax * ay - 1) / (ax * ay)));
         const int alen = (g.Z + az - 1) / az;
         az = (g.Z + alen - 1) / alen;
         k_apply_proj4<<<dim3(ax, ay, az), dim3(32, 8), 0, e.stream>>>(g, alen, e.pp, e.rho, e.u, e.v, e.w);

@@ -1188,7 +1188,7 @@ namespace {
 // of the scratch fields are never read). A single sweep goes through a scratch field.
 // z chunking of a march over gx x gy columns of blocks: about bps blocks per SM in the grid
 inline int z_runs(const Env& e, int gx, int gy, int bps, int& zlen) {
-    int zc = std::max(1, std::min(e.g.Z, (e.num_sms * bps + gx * gy - 1) / (gx * gy)));
+    int zc = std::max(1, std::min(e.g.Z, (stencil_sms(e) * bps + gx * gy - 1) / (gx * gy)));
     zlen = (e.g.Z + zc - 1) / zc;
     return (e.g.Z + zlen - 1) / zlen;
 }
@@ -1288,7 +1288,7 @@ void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float*
     }
     if (npass == 1) {
         const int n4 = g.N / 4;
-        k_copy_sky4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)src, (float4*)f,
+        k_copy_sky4<<<std::min((n4 + 255) / 256, stencil_sms(e) * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)src, (float4*)f,
                                                                                      nullptr, 0);
         e.launches += 1;
     }
@@ -1334,7 +1334,7 @@ void launch_diffuse(Env& e, float* f, int type, float dtS) {
     const float* res = (sweeps % 2 == 0) ? a : o;
     if (vec) {
         const int n4 = g.N / 4;
-        k_copy_sky4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)res, (float4*)f,
+        k_copy_sky4<<<std::min((n4 + 255) / 256, stencil_sms(e) * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, (const float4*)res, (float4*)f,
                                                                                      nullptr, 0);
     } else {
         k_copy_sky<<<cell_grid(g), dim3(BX, BY), 0, e.stream>>>(g, res, f, nullptr, 0);
@@ -1368,7 +1368,7 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
         cudaMemsetAsync(&e.sc->maxbits, 0, sizeof(unsigned int), e.stream);
         if (e.flat && (g.X % 4) == 0) {
             const int n4 = g.N / 4;
-            k_maxvel4<<<std::min((n4 + 255) / 256, e.num_sms * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, g.XY / 4, (const float4*)e.u,
+            k_maxvel4<<<std::min((n4 + 255) / 256, stencil_sms(e) * 8), 256, 0, e.stream>>>(n4, g.X / 4, g.Y, g.XY / 4, (const float4*)e.u,
                                                                                       (const float4*)e.v, (const float4*)e.w,
                                                                                       e.cfg.semantics == 0, e.sc);
         } else {
@@ -1398,23 +1398,23 @@ int launch_advect(Env& e, float* f, const float* def, int sides, int ground, flo
     float* O = e.tA;
     const bool vec = e.flat && (g.X % 4) == 0;
     const int gx = (g.X / 4 + 31) / 32, gy = (g.Y - 1 + DVY - 1) / DVY;
-    int zc = std::max(1, std::min(g.Z, (e.num_sms * e.tune.ppm_bps + gx * gy - 1) / (gx * gy)));
+    int zc = std::max(1, std::min(g.Z, (stencil_sms(e) * e.tune.ppm_bps + gx * gy - 1) / (gx * gy)));
     const int zlen = (g.Z + zc - 1) / zc;
     zc = (g.Z + zlen - 1) / zlen;
     const dim3 vg(gx, gy, zc), vb(32, DVY);
     // the Z pass marches: fewer, longer z chunks
-    int zc2 = std::max(1, std::min(g.Z, (e.num_sms * e.tune.ppmz_bps + gx * gy - 1) / (gx * gy)));
+    int zc2 = std::max(1, std::min(g.Z, (stencil_sms(e) * e.tune.ppmz_bps + gx * gy - 1) / (gx * gy)));
     const int zlen2 = (g.Z + zc2 - 1) / zc2;
     zc2 = (g.Z + zlen2 - 1) / zlen2;
     const dim3 vg2(gx, gy, zc2);
     // the Y pass marches rows in runs
     const int ygz = (g.Z + PY - 1) / PY;
-    int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * e.tune.ppmy_bps + gx * ygz - 1) / (gx * ygz)));
+    int yc = std::max(1, std::min(g.Y - 1, (stencil_sms(e) * e.tune.ppmy_bps + gx * ygz - 1) / (gx * ygz)));
     const int ylen = (g.Y - 1 + yc - 1) / yc;
     yc = (g.Y - 1 + ylen - 1) / ylen;
     const dim3 yg(gx, ygz, yc), yb(32, PY);
     const int n4 = g.N / 4;
-    const int ncopy = std::min((n4 + 255) / 256, e.num_sms * 8);
+    const int ncopy = std::min((n4 + 255) / 256, stencil_sms(e) * 8);
     // one substep (slot i; with chk set, the kernels read the substep count from the device and
     // slots at or beyond it return at once)
     auto substep = [&](int i, const Scalars* chk) {
@@ -1537,7 +1537,7 @@ void launch_buoyancy(Env& e, float dtS) {
     const Grid& g = e.g;
     if (e.flat && (g.X % 4) == 0) {
         const int gx = (g.X / 4 + 31) / 32, gz = (g.Z + BZ4 - 1) / BZ4;
-        int yc = std::max(1, std::min(g.Y - 1, (e.num_sms * 8 + gx * gz - 1) / (gx * gz)));
+        int yc = std::max(1, std::min(g.Y - 1, (stencil_sms(e) * 8 + gx * gz - 1) / (gx * gz)));
         const int ylen = (g.Y - 1 + yc - 1) / yc;
         yc = (g.Y - 1 + ylen - 1) / ylen;
         k_buoyancy4<<<dim3(gx, gz, yc), dim3(32, BZ4), 0, e.stream>>>(g, ylen, e.v, e.th, e.qv, e.qr, e.qs, e.qi, e.p, e.Pg, dtS, dbg);
