@@ -246,8 +246,9 @@ skt_status skt_diffuse_noalloc(int nx, int ny, int nz, float voxel, int field_ty
 /* Launch shapes of the stencil kernels. None of them changes the results (every cell is computed
  * with the same arithmetic from the same neighbour values); they change only the speed.
  * diffuse_depth: sweeps per diffusion pass, 1 or 2 (temporal blocking: two Jacobi sweeps per trip
- * through HBM, input planes streamed by TMA, flat terrain); diffuse_rows: rows per warp of the
- * two-sweep kernel's tile, 4 or 8 (the intermediate sweep is recomputed on the tile's edge rows);
+ * through HBM, input planes streamed by TMA, flat terrain); diffuse_rows selects the two-sweep
+ * kernel and its tile height: 6 or 14 output rows per block of four-cell lanes, or 4 or 8 rows per
+ * warp of one-cell lanes (the intermediate sweep is recomputed on the tile's edge rows);
  * *_bps: blocks per SM in the grid of the diffusion (one-sweep and two-sweep) and PPM (x, y, z
  * pass) marches, which sets their run lengths. from_cache and the times are outputs of
  * skt_autotune. */

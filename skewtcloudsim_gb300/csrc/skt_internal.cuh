@@ -134,7 +134,7 @@ struct SolverCfg {
 // skt_autotune (skt_tune.cu) and otherwise these defaults (hand-measured at 512x256x512).
 struct Tuning {
     int diffuse_depth = 1;   // sweeps per diffusion pass: 1, or 2 (temporal blocking, k_diffuse2)
-    int diffuse_h = 8;       // k_diffuse2: rows per warp (4 or 8)
+    int diffuse_h = 8;       // two-sweep kernel: k_diffuse_pair4 rows per block (6, 14), k_diffuse2 rows per warp (4, 8)
     int diffuse_bps = 32;    // k_diffuse4: blocks per SM in the grid (z-run length)
     int diffuse2_bps = 8;    // k_diffuse2: blocks per SM in the grid (z-run length)
     int ppm_bps = 16;        // k_ppm4x: blocks per SM (z-run length)

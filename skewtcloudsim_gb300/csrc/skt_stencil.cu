@@ -389,6 +389,197 @@ __global__ void __launch_bounds__(32 * D2WARPS) k_diffuse2(const __grid_constant
     }
 }
 
+// Two Jacobi sweeps in one pass with four cells per lane (temporal blocking of depth 2), flat
+// terrain, X % 4 == 0.
+//
+// A block covers 128 x cells (one warp of float4 lanes) by R output rows and marches a run of z
+// planes. Its R + 2 row warps compute the first sweep on rows yb-1 .. yb+R and the inner R of them
+// the second sweep on rows yb .. yb+R-1; one more warp computes the first sweep's cells just left
+// and right of the block (x = bx-1 and bx+128, one lane per row and side), the only cells outside
+// the row warps' lanes that the second sweep reads. The input planes stream through a ring of
+// P4SLOTS shared-memory slots, each filled by one TMA copy of a 136 x (R+4) box: the block's cells
+// with 4 more on either side (the copy starts on a 16-byte boundary) and 2 rows above and below.
+// A lane keeps its own row of two input planes and two first-sweep planes in registers and reads
+// its neighbours (the rows above and below, the cells left and right) from the slot or from two
+// shared planes of the first sweep. Per plane p the block passes one barrier: each warp stores its
+// first-sweep row of plane p, then computes the second sweep of plane p-1 from the shared plane
+// p-1 (complete since the previous barrier); after the barrier the slot of input plane p-1 is
+// refilled. Every cell of either sweep is computed with jacobi() from the same neighbour and ghost
+// values as k_diffuse4, so the pass equals two single sweeps bit for bit.
+constexpr int P4W = 136;    // box width in cells: 4 + 128 + 4 (544 bytes)
+constexpr int P4SLOTS = 6;  // ring depth: planes p-1, p, p+1 in use and three in flight
+template <int R>
+constexpr int p4_slot_bytes() { return ((P4W * (R + 4) * 4 + 127) / 128) * 128; }
+template <int R>
+constexpr int p4_mid_bytes() { return 2 * P4W * (R + 2) * 4; }
+template <int R>
+constexpr int p4_smem_bytes() { return P4SLOTS * p4_slot_bytes<R>() + p4_mid_bytes<R>() + P4SLOTS * 8; }
+template <int R>
+constexpr int p4_min_blocks() { return R >= 14 ? 2 : 4; }  // blocks per SM the registers are budgeted for
+
+__device__ __forceinline__ float4 ld4s(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 zero4() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+__device__ __forceinline__ float4 side4(int bc, float4 c, float d) {
+    return make_float4(side_val(bc, c.x, d), side_val(bc, c.y, d), side_val(bc, c.z, d), side_val(bc, c.w, d));
+}
+// four consecutive cells of a sweep: l and r the x neighbours of the first and the last cell
+__device__ __forceinline__ float4 jacobi4(float4 c, float l, float r, float4 u, float4 d, float4 f, float4 b, float k, float rinv) {
+    return make_float4(jacobi(c.x, l, c.y, u.x, d.x, f.x, b.x, k, rinv), jacobi(c.y, c.x, c.z, u.y, d.y, f.y, b.y, k, rinv),
+                       jacobi(c.z, c.y, c.w, u.z, d.z, f.z, b.z, k, rinv), jacobi(c.w, c.z, r, u.w, d.w, f.w, b.w, k, rinv));
+}
+
+template <bool THETA, int R>
+__global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
+    k_diffuse_pair4(const __grid_constant__ CUtensorMap tin, Grid g, int zlen, float* __restrict__ out, int sides, int ground,
+                    const float* __restrict__ def, float k, const float* __restrict__ face, Scalars* __restrict__ sc) {
+    extern __shared__ __align__(128) unsigned char p4_smem[];
+    constexpr int NR = R + 2;
+    constexpr int SLOTF = p4_slot_bytes<R>() / 4;  // floats per slot
+    constexpr unsigned BOX_BYTES = P4W * (R + 4) * 4;
+    float* const ring = reinterpret_cast<float*>(p4_smem);
+    float* const mid = ring + P4SLOTS * SLOTF;  // [plane & 1][NR rows][P4W]: the first sweep
+    uint64_t* const bar = reinterpret_cast<uint64_t*>(mid + 2 * NR * P4W);
+    const int lane = threadIdx.x, wy = threadIdx.y, tid = lane + 32 * wy;
+    const int X = g.X, Y = g.Y, Z = g.Z, XY = g.XY;
+    const int bx = int(blockIdx.x) * 128, yb = 1 + int(blockIdx.y) * R;
+    const int zs = int(blockIdx.z) * zlen, ze = min(zs + zlen, Z);
+    const int plo = max(zs - 1, 0), phi = min(ze, Z - 1);       // planes of the first sweep
+    const int ilo = max(plo - 1, 0), ihi = min(phi + 1, Z - 1);  // input planes
+    const float rinv = 1.0f / (1 + 6 * k);
+    const float gv = ground == DIRICHLET ? 0.0f : (def ? def[0] : 0.0f);
+    const float4 gv4 = make_float4(gv, gv, gv, gv);
+    // row warps: row y, cells x0 .. x0+3 at column col of a slot row and of a shared plane row
+    const bool edge = wy == NR;
+    const int y = yb - 1 + wy, x0 = bx + 4 * lane, col = 4 + 4 * lane;
+    const bool act = !edge && y >= 1 && y < Y && x0 < X;  // first sweep
+    const bool wr = act && wy >= 1 && wy <= R;             // second sweep, written out
+    const bool yin = y > 1 && y + 1 < Y;                   // no ghost row above or below (warp-uniform)
+    const int own = (wy + 1) * P4W + col, mown = wy * P4W + col;
+    // edge warp: lane 2 er + es holds row yb-1+er at x = bx-1 (es = 0) or bx+128 (es = 1)
+    const int er = lane >> 1, es = lane & 1;
+    const int ey = yb - 1 + er, ex = es ? bx + 128 : bx - 1, eown = (er + 1) * P4W + (es ? 132 : 3);
+    const bool eact = edge && er < NR && ey >= 1 && ey < Y && ex >= 0 && ex < X;
+    const int ry = edge ? ey : y;
+    const float dy = (def && ry >= 0 && ry < Y) ? def[ry] : 0.0f;
+
+    auto issue = [&](int q) {
+        const int s = (q - ilo) % P4SLOTS;
+        mbar_expect_tx(&bar[s], BOX_BYTES);
+        tma_load_3d(ring + s * SLOTF, &tin, &bar[s], bx - 4, yb - 2, q);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < P4SLOTS; ++s) mbar_init(&bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int issued = ilo;  // thread 0: the next input plane to copy
+    if (tid == 0)
+        for (; issued <= min(ihi, ilo + P4SLOTS - 1); ++issued) issue(issued);
+    // the input planes complete in order; wslot / wpar: slot and phase parity of the next one
+    int waited = ilo, wslot = 0;
+    unsigned wpar = 0;
+    bool ok = true;
+    auto wait_to = [&](int q) {
+        for (; waited <= q; ++waited) {
+            if (ok) ok = mbar_wait(&bar[wslot], wpar);
+            if (++wslot == P4SLOTS) {
+                wslot = 0;
+                wpar ^= 1u;
+            }
+        }
+    };
+    auto nxt = [](int s) { return s + 1 == P4SLOTS ? 0 : s + 1; };
+    // first sweep of plane p for a row warp: ib, ic the input planes p-1, p; s0, s1 the slots of p, p+1
+    auto sweep1 = [&](bool gen, int p, const float4& ib, const float4& ic, int s0, int s1, float4& f) {
+        const float* row = ring + s0 * SLOTF + own;
+        f = ld4s(ring + s1 * SLOTF + own);
+        float4 d = ld4s(row - P4W), u = ld4s(row + P4W);
+        float l = row[-1], r = row[4];
+        if (gen) {  // a ghost row or plane: rows 1 and Y-1, the last plane (warp-uniform)
+            if (p + 1 >= Z) f = side4(sides, ic, dy);
+            if (y == 1) d = THETA ? ld4f(face, x0 + p * X) : gv4;
+            if (y + 1 >= Y) u = side4(sides, ic, dy);
+        }
+        if (x0 == 0) l = side_val(sides, ic.x, dy);
+        if (x0 + 4 >= X) r = side_val(sides, ic.w, dy);
+        return jacobi4(ic, l, r, u, d, f, ib, k, rinv);
+    };
+    // second sweep of plane zo from the first sweep's planes mb (zo-1), mc (zo), mf (zo+1)
+    auto sweep2 = [&](bool gen, int zo, const float4& mb, const float4& mc, const float4& mf) {
+        const float* m2 = mid + (zo & 1) * (NR * P4W) + mown;
+        float4 d = ld4s(m2 - P4W), u = ld4s(m2 + P4W);
+        float l = m2[-1], r = m2[4];
+        if (gen) {
+            if (y == 1) d = THETA ? ld4f(face, x0 + zo * X) : gv4;
+            if (y + 1 >= Y) u = side4(sides, mc, dy);
+        }
+        if (x0 == 0) l = side_val(sides, mc.x, dy);
+        if (x0 + 4 >= X) r = side_val(sides, mc.w, dy);
+        *reinterpret_cast<float4*>(out + x0 + y * X + zo * XY) = jacobi4(mc, l, r, u, d, mf, mb, k, rinv);
+    };
+
+    float4 ib = zero4(), ic = zero4(), mb = zero4(), mc = zero4();  // input planes p-1, p; first sweep p-2, p-1
+    int s0 = (plo - ilo) % P4SLOTS;                                  // the slot of plane p
+    wait_to(plo);
+    if (act && ok) {
+        ic = ld4s(ring + s0 * SLOTF + own);
+        ib = plo >= 1 ? ld4s(ring + (plo - 1 - ilo) * SLOTF + own) : side4(sides, ic, dy);
+    }
+    bool stuck = false;
+    for (int p = plo; p <= phi; ++p) {
+        wait_to(min(p + 1, ihi));
+        const int s1 = nxt(s0);
+        if (ok) {
+            float4 mf = zero4();
+            if (act) {
+                float4 f;
+                const bool gen = !yin || p + 1 >= Z;
+                mf = gen ? sweep1(true, p, ib, ic, s0, s1, f) : sweep1(false, p, ib, ic, s0, s1, f);
+                *reinterpret_cast<float4*>(mid + (p & 1) * (NR * P4W) + mown) = mf;
+                ib = ic;
+                ic = f;
+            }
+            if (eact) {  // the left cell's left neighbour is inside the grid (bx >= 128), as is the right cell's
+                const float* row = ring + s0 * SLOTF + eown;
+                const float c = row[0];
+                const float r = ex + 1 < X ? row[1] : side_val(sides, c, dy);
+                const float d = ey > 1 ? row[-P4W] : (THETA ? __ldg(face + ex + p * X) : gv);
+                const float u = ey + 1 < Y ? row[P4W] : side_val(sides, c, dy);
+                const float f = p + 1 < Z ? ring[s1 * SLOTF + eown] : side_val(sides, c, dy);
+                const float b = p >= 1 ? ring[(s0 == 0 ? P4SLOTS - 1 : s0 - 1) * SLOTF + eown] : side_val(sides, c, dy);
+                mid[(p & 1) * (NR * P4W) + er * P4W + (es ? 132 : 3)] = jacobi(c, row[-1], r, u, d, f, b, k, rinv);
+            }
+            if (wr && p - 1 >= zs) {
+                if (yin) sweep2(false, p - 1, mb, mc, mf);
+                else sweep2(true, p - 1, mb, mc, mf);
+            }
+            mb = mc;
+            mc = mf;
+            if (p == 0) mb = side4(sides, mc, dy);  // the first sweep's ghost plane z = -1
+        }
+        // the first sweep of plane p is complete and slot p-1 is read (a stuck copy stops the block)
+        if (__syncthreads_or(!ok)) {
+            stuck = true;
+            break;
+        }
+        if (tid == 0 && p - 1 >= ilo && issued <= ihi) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(issued++);
+        }
+        s0 = s1;
+    }
+    if (!stuck && ze == Z && wr && Z - 1 >= zs) sweep2(true, Z - 1, mb, mc, side4(sides, mc, dy));  // plane Z-1: z+1 is the ghost
+    if (stuck && tid == 0) {
+        // record the timeout, then let the copies still in flight land before the block's shared
+        // memory goes away (each wait again bounded)
+        sc->status = SKT_TIMEOUT;
+        for (int q = max(issued - P4SLOTS, ilo); q < issued; ++q) {
+            const int rel = q - ilo;
+            (void)mbar_wait(&bar[rel % P4SLOTS], unsigned(rel / P4SLOTS) & 1u);
+        }
+    }
+}
+
 // advectPPMFlux, Game/kernelSky.cu:270-366 (van Leer slope, Walcek limiter, Courant clamp),
 // written without branches: the limiter ratios are formed unconditionally and selected, the
 // parabola's sign case by a select. cdt = dt/vox: the Courant number is veli*cdt (the reference
@@ -1209,13 +1400,13 @@ TensorMapEncodeFn tensor_map_encoder() {
     return fn;
 }
 
-// A field as a 3D tensor (x fastest) read in boxes of 36 x rows x 1 cells; false if it cannot be encoded.
-bool field_tensor_map(const Grid& g, const float* base, int rows, CUtensorMap* map) {
+// A field as a 3D tensor (x fastest) read in boxes of width x rows x 1 cells; false if it cannot be encoded.
+bool field_tensor_map(const Grid& g, const float* base, int width, int rows, CUtensorMap* map) {
     TensorMapEncodeFn enc = tensor_map_encoder();
     if (!enc) return false;
     const cuuint64_t dims[3] = {cuuint64_t(g.X), cuuint64_t(g.Y), cuuint64_t(g.Z)};
     const cuuint64_t strides[2] = {cuuint64_t(g.X) * 4, cuuint64_t(g.XY) * 4};
-    const cuuint32_t box[3] = {cuuint32_t(D2BW), cuuint32_t(rows), 1};
+    const cuuint32_t box[3] = {cuuint32_t(width), cuuint32_t(rows), 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
@@ -1226,7 +1417,7 @@ bool launch_diffuse2(Env& e, int bps, const float* src, float* dst, int sides, i
                      const float* face) {
     const Grid& g = e.g;
     CUtensorMap map;
-    if (!field_tensor_map(g, src, d2_box_rows<H>(), &map)) return false;
+    if (!field_tensor_map(g, src, D2BW, d2_box_rows<H>(), &map)) return false;
     const int gx = (g.X + D2OUT - 1) / D2OUT, gy = (g.Y - 1 + H * D2WARPS - 1) / (H * D2WARPS);
     int zlen;
     const int zc = z_runs(e, gx, gy, bps, zlen);
@@ -1238,6 +1429,39 @@ bool launch_diffuse2(Env& e, int bps, const float* src, float* dst, int sides, i
     }
     k_diffuse2<THETA, H><<<dim3(gx, gy, zc), dim3(32, D2WARPS), smem, e.stream>>>(map, g, zlen, dst, sides, ground, def, k, face, e.sc);
     return true;
+}
+
+template <bool THETA, int R>
+bool launch_diffuse_pair4(Env& e, int bps, const float* src, float* dst, int sides, int ground, const float* def, float k,
+                          const float* face) {
+    const Grid& g = e.g;
+    CUtensorMap map;
+    if (!field_tensor_map(g, src, P4W, R + 4, &map)) return false;
+    const int gx = (g.X + 127) / 128, gy = (g.Y - 1 + R - 1) / R;
+    int zlen;
+    const int zc = z_runs(e, gx, gy, bps, zlen);
+    constexpr int smem = p4_smem_bytes<R>();
+    static bool attr = false;  // per template instance
+    if (!attr) {
+        cudaFuncSetAttribute(k_diffuse_pair4<THETA, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+    }
+    k_diffuse_pair4<THETA, R><<<dim3(gx, gy, zc), dim3(32, R + 3), smem, e.stream>>>(map, g, zlen, dst, sides, ground, def, k, face,
+                                                                                    e.sc);
+    return true;
+}
+
+// one pass of two sweeps with the tuned kernel: k_diffuse_pair4 (float4 lanes, rows 6 or 14 per
+// block) or k_diffuse2 (one cell per lane, rows 4 or 8 per warp); false without a tensor map
+template <bool THETA>
+bool launch_pair(Env& e, const float* src, float* dst, int sides, int ground, const float* def, float k, const float* face) {
+    const int h = e.tune.diffuse_h, bps = e.tune.diffuse2_bps;
+    switch (h) {
+        case 14: return launch_diffuse_pair4<THETA, 14>(e, bps, src, dst, sides, ground, def, k, face);
+        case 6: return launch_diffuse_pair4<THETA, 6>(e, bps, src, dst, sides, ground, def, k, face);
+        case 8: return launch_diffuse2<THETA, 8>(e, bps, src, dst, sides, ground, def, k, face);
+        default: return launch_diffuse2<THETA, 4>(e, bps, src, dst, sides, ground, def, k, face);
+    }
 }
 
 void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float* def, float k, int sweeps) {
@@ -1260,14 +1484,8 @@ void diffuse_vec(Env& e, float* f, int type, int sides, int ground, const float*
         float* dst = (q == npass - 1 && q > 0) ? f : buf[q % 2];
         const bool two = pairs && !(q == 0 && sweeps % 2 == 1);
         if (two) {
-            const int h = e.tune.diffuse_h, bps = e.tune.diffuse2_bps;
-            bool ok;
-            if (type == 0)
-                ok = h == 8 ? launch_diffuse2<true, 8>(e, bps, src, dst, sides, ground, def, k, face)
-                            : launch_diffuse2<true, 4>(e, bps, src, dst, sides, ground, def, k, face);
-            else
-                ok = h == 8 ? launch_diffuse2<false, 8>(e, bps, src, dst, sides, ground, def, k, nullptr)
-                            : launch_diffuse2<false, 4>(e, bps, src, dst, sides, ground, def, k, nullptr);
+            const bool ok = type == 0 ? launch_pair<true>(e, src, dst, sides, ground, def, k, face)
+                                      : launch_pair<false>(e, src, dst, sides, ground, def, k, nullptr);
             if (!ok) {  // no tensor-map encoder: the two sweeps as two passes
                 if (type == 0) {
                     k_diffuse4<true><<<dim3(vx, vy, vz), dim3(32, DVY), 0, e.stream>>>(g, vlen, src, buf[2], sides, ground, def, k, face);

@@ -41,7 +41,7 @@ void to_abi(const Tuning& t, skt_tuning* o) {
 
 bool from_abi(const skt_tuning* o, Tuning& t) {
     auto in = [](int v, int lo, int hi) { return v >= lo && v <= hi; };
-    if (!(o->diffuse_depth == 1 || o->diffuse_depth == 2) || !(o->diffuse_rows == 4 || o->diffuse_rows == 8) ||
+    if (!(o->diffuse_depth == 1 || o->diffuse_depth == 2) || !(o->diffuse_rows == 4 || o->diffuse_rows == 8 || o->diffuse_rows == 6 || o->diffuse_rows == 14) ||
         !in(o->diffuse_bps, 1, 256) || !in(o->diffuse2_bps, 1, 256) || !in(o->ppm_x_bps, 1, 256) || !in(o->ppm_y_bps, 1, 256) ||
         !in(o->ppm_z_bps, 1, 256))
         return false;
@@ -157,7 +157,7 @@ skt_status skt_set_tuning(skt_env* env, const skt_tuning* t) {
     if (!env || !t) return report(env ? &env->e : nullptr, SKT_INVALID_ARG, "null argument");
     Tuning nt = env->e.tune;
     if (!from_abi(t, nt))
-        return report(&env->e, SKT_INVALID_ARG, "invalid tuning (diffuse_depth 1 or 2, diffuse_rows 4 or 8, blocks per SM 1..256)");
+        return report(&env->e, SKT_INVALID_ARG, "invalid tuning (diffuse_depth 1 or 2, diffuse_rows 4, 6, 8 or 14, blocks per SM 1..256)");
     env->e.tune = nt;
     return SKT_OK;
 }
@@ -213,8 +213,12 @@ skt_status skt_autotune(skt_env* env, const char* cache_path, int flags, skt_tun
     std::vector<Cand> cands;
     for (int bps : {16, 32, 64}) cands.push_back({1, base.diffuse_h, bps});
     if (e.flat && (e.g.X % 4) == 0 && e.cfg.diffuse_sweeps >= 2)
+    {
+        for (int bps : {2, 4, 8}) cands.push_back({2, 14, bps});
+        for (int bps : {4, 8}) cands.push_back({2, 6, bps});
         for (int h : {4, 8})
             for (int bps : {4, 8, 16}) cands.push_back({2, h, bps});
+    }
     Tuning best = base;
     float best_ms = 1e30f;
     for (const Cand& c : cands) {

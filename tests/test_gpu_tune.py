@@ -1,11 +1,13 @@
 """Launch-shape tuning (skt_set_tuning / skt_autotune) and the two-sweep diffusion kernel.
 
-The tuned shapes must not change a single bit: the two-sweep pass (temporal blocking of depth 2,
-k_diffuse2, input planes streamed through shared memory by TMA) recomputes each intermediate
-cell with the arithmetic of the one-sweep kernel from the same neighbour values, its ghost values
-included, so every diffusion boundary table, even and odd sweep counts, both tile heights and
-several run lengths are compared bit for bit with the default one-sweep passes, on a 32^3 grid
-and on a wide one (x = 260: several tiles, a ragged last tile, several z runs). k = 0.1
+The tuned shapes must not change a single bit: the two-sweep passes (temporal blocking of depth
+2, input planes streamed through shared memory by TMA: k_diffuse_pair4 with four-cell lanes and
+6 or 14 rows per block, k_diffuse2 with one-cell lanes and 4 or 8 rows per warp) compute each
+intermediate cell with the arithmetic of the one-sweep kernel from the same neighbour values, its
+ghost values included, so every diffusion boundary table, even and odd sweep counts, every tile
+height and several run lengths (down to one plane per run) are compared bit for bit with the
+default one-sweep passes, on a 32^3 grid and on a wide one (x = 260: three blocks along x, the
+last with one active lane, ragged row tiles, several z runs). k = 0.1
 (dt*speed = 2e5 s) makes every neighbour term count. The autotuner is checked to write its cache,
 to read it back for a second environment of the same grid, and to leave a whole step's results
 unchanged.
@@ -34,7 +36,9 @@ def _developed_env(shape, cfg):
 def test_two_sweep_diffusion_is_bit_identical(gpu_lib, shape, sweeps):
     init, dt, speed, ref = _developed_env(shape, gpu_cfg(0, diffuse_sweeps=sweeps))
     state = {k: ref.read(k) for k in SKY + GROUND}  # theta's ground faces read the ground T and p
-    variants = [dict(diffuse_depth=2, diffuse_rows=4, diffuse2_bps=8), dict(diffuse_depth=2, diffuse_rows=8, diffuse2_bps=2),
+    variants = [dict(diffuse_depth=2, diffuse_rows=14, diffuse2_bps=2), dict(diffuse_depth=2, diffuse_rows=14, diffuse2_bps=64),
+                dict(diffuse_depth=2, diffuse_rows=6, diffuse2_bps=4), dict(diffuse_depth=2, diffuse_rows=6, diffuse2_bps=256),
+                dict(diffuse_depth=2, diffuse_rows=4, diffuse2_bps=8), dict(diffuse_depth=2, diffuse_rows=8, diffuse2_bps=2),
                 dict(diffuse_depth=2, diffuse_rows=4, diffuse2_bps=64), dict(diffuse_depth=1, diffuse_bps=7)]
     envs = []
     for v in variants:
@@ -96,6 +100,8 @@ def test_set_tuning_rejects_bad_values(gpu_lib):
         env.set_tuning(diffuse_depth=3)
     with pytest.raises(SktError):
         env.set_tuning(diffuse_rows=5)
+    with pytest.raises(SktError):
+        env.set_tuning(diffuse_rows=12)
     with pytest.raises(SktError):
         env.set_tuning(ppm_x_bps=0)
     env.close()
