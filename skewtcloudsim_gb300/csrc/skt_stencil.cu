@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 namespace skt {
 
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(32 * D2WARPS) k_diffuse2(const __grid_constant
 // refilled. Every cell of either sweep is computed with jacobi() from the same neighbour and ghost
 // values as k_diffuse4, so the pass equals two single sweeps bit for bit.
 constexpr int P4W = 136;    // box width in cells: 4 + 128 + 4 (544 bytes)
-constexpr int P4SLOTS = 6;  // ring depth: planes p-1, p, p+1 in use and three in flight
+constexpr int P4SLOTS = 8;  // ring depth: planes p-1, p, p+1 in use and five in flight
 template <int R>
 constexpr int p4_slot_bytes() { return ((P4W * (R + 4) * 4 + 127) / 128) * 128; }
 template <int R>
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
     float* const ring = reinterpret_cast<float*>(p4_smem);
     float* const mid = ring + P4SLOTS * SLOTF;  // [plane & 1][NR rows][P4W]: the first sweep
     uint64_t* const bar = reinterpret_cast<uint64_t*>(mid + 2 * NR * P4W);
-    const int lane = threadIdx.x, wy = threadIdx.y, tid = lane + 32 * wy;
+    const int tid = threadIdx.x, lane = tid & 31, wy = tid >> 5;  // a 1D block: the warp index is warp-uniform
     const int X = g.X, Y = g.Y, Z = g.Z, XY = g.XY;
     const int bx = int(blockIdx.x) * 128, yb = 1 + int(blockIdx.y) * R;
     const int zs = int(blockIdx.z) * zlen, ze = min(zs + zlen, Z);
@@ -451,10 +452,12 @@ __global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
     // row warps: row y, cells x0 .. x0+3 at column col of a slot row and of a shared plane row
     const bool edge = wy == NR;
     const int y = yb - 1 + wy, x0 = bx + 4 * lane, col = 4 + 4 * lane;
-    const bool act = !edge && y >= 1 && y < Y && x0 < X;  // first sweep
-    const bool wr = act && wy >= 1 && wy <= R;             // second sweep, written out
+    const bool act = !edge && y >= 1 && y < Y;  // first sweep (warp-uniform; lanes past X compute unused values)
+    const bool wr = act && wy >= 1 && wy <= R;   // second sweep (written out for x0 < X)
+    const bool xin = x0 < X;
     const bool yin = y > 1 && y + 1 < Y;                   // no ghost row above or below (warp-uniform)
     const int own = (wy + 1) * P4W + col, mown = wy * P4W + col;
+    const bool lfix = x0 == 0, rfix = x0 + 4 >= X;  // the x ghosts of the first and last cell
     // edge warp: lane 2 er + es holds row yb-1+er at x = bx-1 (es = 0) or bx+128 (es = 1)
     const int er = lane >> 1, es = lane & 1;
     const int ey = yb - 1 + er, ex = es ? bx + 128 : bx - 1, eown = (er + 1) * P4W + (es ? 132 : 3);
@@ -479,66 +482,124 @@ __global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
     int waited = ilo, wslot = 0;
     unsigned wpar = 0;
     bool ok = true;
-    auto wait_to = [&](int q) {
-        for (; waited <= q; ++waited) {
-            if (ok) ok = mbar_wait(&bar[wslot], wpar);
-            if (++wslot == P4SLOTS) {
-                wslot = 0;
-                wpar ^= 1u;
-            }
+    auto wait_next = [&]() {  // waits for input plane `waited`
+        if (!mbar_try_wait(&bar[wslot], wpar)) ok = mbar_wait(&bar[wslot], wpar) && ok;
+        ++waited;
+        if (++wslot == P4SLOTS) {
+            wslot = 0;
+            wpar ^= 1u;
         }
     };
     auto nxt = [](int s) { return s + 1 == P4SLOTS ? 0 : s + 1; };
     // first sweep of plane p for a row warp: ib, ic the input planes p-1, p; s0, s1 the slots of p, p+1
-    auto sweep1 = [&](bool gen, int p, const float4& ib, const float4& ic, int s0, int s1, float4& f) {
+    // x neighbours of a lane's four cells c from the shared row (at the warp's ends the edge warp's
+    // cells), at the grid's ends the ghost. (Warp shuffles for the inner lanes measured slower: the
+    // end lanes' loads become divergent branches.)
+    auto xnb = [&](const float4& c, const float* row, float& l, float& r) {
+        l = lfix ? side_val(sides, c.x, dy) : row[-1];
+        r = rfix ? side_val(sides, c.w, dy) : row[4];
+    };
+    // dg: the value below row 1 (theta's ground face of the plane, else the ground ghost)
+    auto sweep1 = [&](bool gen, int p, const float4& ib, const float4& ic, int s0, int s1, float4& f, const float4& dg) {
         const float* row = ring + s0 * SLOTF + own;
         f = ld4s(ring + s1 * SLOTF + own);
         float4 d = ld4s(row - P4W), u = ld4s(row + P4W);
-        float l = row[-1], r = row[4];
         if (gen) {  // a ghost row or plane: rows 1 and Y-1, the last plane (warp-uniform)
             if (p + 1 >= Z) f = side4(sides, ic, dy);
-            if (y == 1) d = THETA ? ld4f(face, x0 + p * X) : gv4;
+            if (y == 1) d = dg;
             if (y + 1 >= Y) u = side4(sides, ic, dy);
         }
-        if (x0 == 0) l = side_val(sides, ic.x, dy);
-        if (x0 + 4 >= X) r = side_val(sides, ic.w, dy);
+        float l, r;
+        xnb(ic, row, l, r);
         return jacobi4(ic, l, r, u, d, f, ib, k, rinv);
     };
     // second sweep of plane zo from the first sweep's planes mb (zo-1), mc (zo), mf (zo+1)
-    auto sweep2 = [&](bool gen, int zo, const float4& mb, const float4& mc, const float4& mf) {
+    auto sweep2 = [&](bool gen, int zo, const float4& mb, const float4& mc, const float4& mf, bool store, const float4& dg) {
         const float* m2 = mid + (zo & 1) * (NR * P4W) + mown;
         float4 d = ld4s(m2 - P4W), u = ld4s(m2 + P4W);
-        float l = m2[-1], r = m2[4];
         if (gen) {
-            if (y == 1) d = THETA ? ld4f(face, x0 + zo * X) : gv4;
+            if (y == 1) d = dg;
             if (y + 1 >= Y) u = side4(sides, mc, dy);
         }
-        if (x0 == 0) l = side_val(sides, mc.x, dy);
-        if (x0 + 4 >= X) r = side_val(sides, mc.w, dy);
-        *reinterpret_cast<float4*>(out + x0 + y * X + zo * XY) = jacobi4(mc, l, r, u, d, mf, mb, k, rinv);
+        float l, r;
+        xnb(mc, m2, l, r);
+        const float4 o = jacobi4(mc, l, r, u, d, mf, mb, k, rinv);
+        if (xin && store) *reinterpret_cast<float4*>(out + x0 + y * X + zo * XY) = o;
     };
 
+    // Every warp runs the plane steps p = plo .. phi with one barrier each; the row warps that
+    // sweep and the other warps (the edge warp, rows outside the grid) run separate loops, so that
+    // neither tests its role per step.
+    auto refill = [&](int p) {  // thread 0, after the barrier of step p: slot p-1 takes plane p-1+P4SLOTS
+        if (tid == 0 && p - 1 >= ilo && issued <= ihi) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(issued++);
+        }
+    };
+    int s0 = (plo - ilo) % P4SLOTS;  // the slot of plane p
+    bool stuck = false;
+    wait_next();  // plane ilo
+    if (plo > ilo) wait_next();
+    // one plane step of a row warp: the first sweep of plane p, the second of plane p-1, the
+    // barrier and the refill; false when a copy got stuck. G1 / G2: the first / second sweep may
+    // meet a ghost row or plane (rows 1 and Y-1, the grid's last plane); WR: the warp writes the
+    // second sweep; GEN: the grid's first or last plane (tests everything at run time).
     float4 ib = zero4(), ic = zero4(), mb = zero4(), mc = zero4();  // input planes p-1, p; first sweep p-2, p-1
-    int s0 = (plo - ilo) % P4SLOTS;                                  // the slot of plane p
-    wait_to(plo);
-    if (act && ok) {
+    // row 1 of theta: the ground face of plane p (gc), loaded a step ahead; only the rows next to a
+    // ghost row (G1) carry it
+    const bool face_row = THETA && y == 1 && xin;
+    auto face_at = [&](int z) { return face_row ? ld4f(face, x0 + z * X) : gv4; };
+    auto row_step = [&](auto g1_c, auto g2_c, auto wr_c, auto gen_c, int p, float4& gc) {
+        constexpr bool G1 = decltype(g1_c)::value, G2 = decltype(g2_c)::value, WR = decltype(wr_c)::value;
+        constexpr bool GEN = decltype(gen_c)::value;
+        if (!GEN || p + 1 <= ihi) wait_next();  // plane p+1
+        const int s1 = nxt(s0);
+        float4 f;
+        const float4 g1 = gc;
+        if (G1) gc = p + 1 < Z ? face_at(p + 1) : gv4;  // the next plane's face, loaded a step ahead
+        const float4 mf = sweep1(G1, p, ib, ic, s0, s1, f, g1);
+        *reinterpret_cast<float4*>(mid + (p & 1) * (NR * P4W) + mown) = mf;
+        ib = ic;
+        ic = f;
+        // written from the run's first plane on; the face of plane p-1 was read a step ago (L1)
+        if (WR) sweep2(G2, p - 1, mb, mc, mf, p - 1 >= zs, (G2 && p >= 1) ? face_at(p - 1) : gv4);
+        mb = (GEN && p == 0) ? side4(sides, mf, dy) : mc;     // plane 0: the first sweep's ghost plane z = -1
+        mc = mf;
+        // the first sweep of plane p is complete and slot p-1 is read (a stuck copy stops the block)
+        if (__syncthreads_or(!ok)) return false;
+        refill(p);
+        s0 = s1;
+        return true;
+    };
+    auto rows = [&](auto ye_c, auto wr_c) {  // YE: the row has a ghost row above or below
+        constexpr bool YE = decltype(ye_c)::value;
+        using T = std::true_type;
+        using F = std::false_type;
         ic = ld4s(ring + s0 * SLOTF + own);
         ib = plo >= 1 ? ld4s(ring + (plo - 1 - ilo) * SLOTF + own) : side4(sides, ic, dy);
-    }
-    bool stuck = false;
-    for (int p = plo; p <= phi; ++p) {
-        wait_to(min(p + 1, ihi));
-        const int s1 = nxt(s0);
-        if (ok) {
-            float4 mf = zero4();
-            if (act) {
-                float4 f;
-                const bool gen = !yin || p + 1 >= Z;
-                mf = gen ? sweep1(true, p, ib, ic, s0, s1, f) : sweep1(false, p, ib, ic, s0, s1, f);
-                *reinterpret_cast<float4*>(mid + (p & 1) * (NR * P4W) + mown) = mf;
-                ib = ic;
-                ic = f;
-            }
+        float4 gc = gv4;  // the face of plane p (rows next to a ghost row)
+        if (YE) gc = face_at(plo);
+        int p = plo;
+        if (p == 0 && p <= phi && !row_step(T{}, T{}, wr_c, T{}, p++, gc)) return false;
+        const int pend = phi == Z - 1 ? phi - 1 : phi;  // the grid's last plane runs the general step
+        for (; p <= pend; ++p)
+            if (!row_step(std::integral_constant<bool, YE>{}, std::integral_constant<bool, YE>{}, wr_c, F{}, p, gc)) return false;
+        for (; p <= phi; ++p)
+            if (!row_step(T{}, T{}, wr_c, T{}, p, gc)) return false;
+        if (ze == Z && decltype(wr_c)::value) sweep2(true, Z - 1, mb, mc, side4(sides, mc, dy), Z - 1 >= zs, face_at(Z - 1));  // z+1 of Z-1: the ghost
+        return true;
+    };
+    if (act) {
+        using T = std::true_type;
+        using F = std::false_type;
+        bool fine;
+        if (yin) fine = wr ? rows(F{}, T{}) : rows(F{}, F{});
+        else fine = wr ? rows(T{}, T{}) : rows(T{}, F{});
+        stuck = !fine;
+    } else {
+        for (int p = plo; p <= phi; ++p) {
+            if (p + 1 <= ihi) wait_next();
+            const int s1 = nxt(s0);
             if (eact) {  // the left cell's left neighbour is inside the grid (bx >= 128), as is the right cell's
                 const float* row = ring + s0 * SLOTF + eown;
                 const float c = row[0];
@@ -549,26 +610,14 @@ __global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
                 const float b = p >= 1 ? ring[(s0 == 0 ? P4SLOTS - 1 : s0 - 1) * SLOTF + eown] : side_val(sides, c, dy);
                 mid[(p & 1) * (NR * P4W) + er * P4W + (es ? 132 : 3)] = jacobi(c, row[-1], r, u, d, f, b, k, rinv);
             }
-            if (wr && p - 1 >= zs) {
-                if (yin) sweep2(false, p - 1, mb, mc, mf);
-                else sweep2(true, p - 1, mb, mc, mf);
+            if (__syncthreads_or(!ok)) {
+                stuck = true;
+                break;
             }
-            mb = mc;
-            mc = mf;
-            if (p == 0) mb = side4(sides, mc, dy);  // the first sweep's ghost plane z = -1
+            refill(p);
+            s0 = s1;
         }
-        // the first sweep of plane p is complete and slot p-1 is read (a stuck copy stops the block)
-        if (__syncthreads_or(!ok)) {
-            stuck = true;
-            break;
-        }
-        if (tid == 0 && p - 1 >= ilo && issued <= ihi) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(issued++);
-        }
-        s0 = s1;
     }
-    if (!stuck && ze == Z && wr && Z - 1 >= zs) sweep2(true, Z - 1, mb, mc, side4(sides, mc, dy));  // plane Z-1: z+1 is the ghost
     if (stuck && tid == 0) {
         // record the timeout, then let the copies still in flight land before the block's shared
         // memory goes away (each wait again bounded)
@@ -1446,7 +1495,7 @@ bool launch_diffuse_pair4(Env& e, int bps, const float* src, float* dst, int sid
         cudaFuncSetAttribute(k_diffuse_pair4<THETA, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         attr = true;
     }
-    k_diffuse_pair4<THETA, R><<<dim3(gx, gy, zc), dim3(32, R + 3), smem, e.stream>>>(map, g, zlen, dst, sides, ground, def, k, face,
+    k_diffuse_pair4<THETA, R><<<dim3(gx, gy, zc), 32 * (R + 3), smem, e.stream>>>(map, g, zlen, dst, sides, ground, def, k, face,
                                                                                     e.sc);
     return true;
 }
