@@ -261,7 +261,7 @@ typedef struct {
     int ppm_y_bps;
     int ppm_z_bps;
     int from_cache;   /* skt_autotune: 1 when the shapes came from the cache file */
-    float diffuse_ms; /* skt_autotune: one diffusion (all sweeps) with the chosen shapes */
+    float diffuse_ms; /* skt_autotune: theta's and water vapour's diffusions (all sweeps) with the chosen shapes */
     float advect_ms;  /* skt_autotune: one advection (all passes and substeps) with the chosen shapes */
 } skt_tuning;
 
