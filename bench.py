@@ -256,16 +256,26 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def step_bytes(mode, pcg_iters, outer):
-    """Algorithmic bytes per cell-step of the whole step (FP32, one advection substep): the stage
-    total of the hot-path scope (2534 B; the three falling species share one march, 36 B instead
-    of 3 x 20) plus the pressure solve. Plain Jacobi-PCG: 60 B per iteration (the operator with
-    the search step and the pressure update 40 B, the residual update with z = r/diag 20 B). Mixed: per inner iteration the operator + search (32 B), the update (24 B) and the
-    V-cycle (93 B: four finest-level passes of 16-24.5 B with FP16 coefficients plus the coarser
-    levels), per refinement step the float-float residual (32 B) and the correction (20 B)."""
+DIFFUSION_BYTES = 1600.0  # 10 fields x 20 sweeps x (4 B read + 4 B written) at one sweep per pass
+
+
+def stage_bytes(diffuse_depth=1):
+    """The library's stage bytes per cell-step (FP32, one advection substep): the hot-path scope's
+    stage total with the three falling species in one march (36 B instead of 3 x 20): 2534 B, of
+    which the diffusion is 1600 B at one sweep per pass and half that with two sweeps per pass."""
+    return 2534.0 - DIFFUSION_BYTES + DIFFUSION_BYTES / max(diffuse_depth, 1)
+
+
+def step_bytes(mode, pcg_iters, outer, diffuse_depth=1):
+    """Algorithmic bytes per cell-step of the whole step as the library moves them: the stages
+    (stage_bytes) plus the pressure solve. Plain Jacobi-PCG: 60 B per iteration (the operator with
+    the search step and the pressure update 40 B, the residual update with z = r/diag 20 B). Mixed:
+    per inner iteration the operator + search (32 B), the update (24 B) and the V-cycle (93 B: four
+    finest-level passes of 16-24.5 B with FP16 coefficients plus the coarser levels), per
+    refinement step the float-float residual (32 B) and the correction (20 B)."""
     if mode == "plain":
-        return 2534.0 + 60.0 * pcg_iters
-    return 2534.0 + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
+        return stage_bytes(diffuse_depth) + 60.0 * pcg_iters
+    return stage_bytes(diffuse_depth) + (32.0 + 24.0 + 93.0) * pcg_iters + 52.0 * max(outer, 1)
 
 
 # plain_textbook: the plain Jacobi-PCG on the textbook (symmetric) operator the mixed mode solves,
@@ -489,10 +499,12 @@ def main():
             roofline["traffic_source"] = ("ncu DRAM bytes read + written by one launch at 512x256x256, scaled to this "
                                           "launch's cells (bytes per launch)")
     step_ms_prof = sum(v["ms"] for v in prof.values())
-    bstep = step_bytes(head["mode"], head["pcg_iters"], head["outer"])
+    depth = head["tuning"].get("diffuse_depth", 1)
+    bstep = step_bytes(head["mode"], head["pcg_iters"], head["outer"], depth)
     step_model = {"bytes_per_cell_step": bstep, "achieved_gbs": round(bstep * head["value"] / 1e9, 1),
                   "frac": round(bstep * head["value"] / 1e9 / peak, 4), "peak_source": peak_kind,
-                  "model": "the library's own bytes: 2534 B of stages + 60 B per plain PCG iteration (stored coefficients)"}
+                  "model": (f"the library's own bytes: {stage_bytes(depth):.0f} B of stages (diffusion at {depth} sweep(s) per "
+                            "pass) + 60 B per plain PCG iteration (stored coefficients)")}
     if head["mode"] != "mixed":
         sb = survey_step_bytes(head["mode"], head["pcg_iters"], head["outer"])
         step_model["scope_model"] = {
@@ -564,8 +576,9 @@ def main():
             "pcg_max_iter": t["pcg_max_iter"], "gpu_launches": t["launches"], "clocks": t["clocks"],
             "note": "the plain Jacobi-PCG on the textbook (symmetric) operator the mixed mode solves, run without the "
                     "iteration cap to the reference's stop test max |r| <= 1e-5",
-            "step_roofline": {"bytes_per_cell_step": step_bytes("plain", t["pcg_iters"], 0),
-                              "frac": round(step_bytes("plain", t["pcg_iters"], 0) * t["value"] / 1e9 / peak, 4),
+            "step_roofline": {"bytes_per_cell_step": step_bytes("plain", t["pcg_iters"], 0, t["tuning"].get("diffuse_depth", 1)),
+                              "frac": round(step_bytes("plain", t["pcg_iters"], 0, t["tuning"].get("diffuse_depth", 1)) * t["value"]
+                                            / 1e9 / peak, 4),
                               "scope_model_frac": round(survey_step_bytes("plain", t["pcg_iters"], 0) * t["value"] / 1e9 / peak, 4)},
             "profile_ms": {k: round(v["ms"], 3) for k, v in t["prof"].items()}}
     if "mixed" in res and head["mode"] != "mixed":
@@ -573,8 +586,9 @@ def main():
         out["mixed"] = {"value": m["value"], "ms_per_step": m["ms_per_step"], "speedup_vs_plain": round(m["value"] / head["value"], 3),
                         "semantics": m["semantics"], "inner_iters_per_step": m["pcg_iters"], "refine_steps": m["outer"],
                         "converged": m["converged"], "rel_residual": m["residual"], "gpu_launches": m["launches"],
-                        "step_roofline": {"bytes_per_cell_step": step_bytes("mixed", m["pcg_iters"], m["outer"]),
-                                          "frac": round(step_bytes("mixed", m["pcg_iters"], m["outer"]) * m["value"] / 1e9 / peak, 4)},
+                        "step_roofline": {"bytes_per_cell_step": step_bytes("mixed", m["pcg_iters"], m["outer"], m["tuning"].get("diffuse_depth", 1)),
+                                          "frac": round(step_bytes("mixed", m["pcg_iters"], m["outer"], m["tuning"].get("diffuse_depth", 1))
+                                                        * m["value"] / 1e9 / peak, 4)},
                         "clocks": m["clocks"], "profile_ms": {k: round(v["ms"], 3) for k, v in m["prof"].items()}}
         if "plain_textbook" in res:
             out["mixed"]["speedup_vs_plain_textbook"] = round(m["value"] / res["plain_textbook"]["value"], 3)

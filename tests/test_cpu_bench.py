@@ -26,6 +26,7 @@ def test_step_byte_model():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.step_bytes("plain", 200, 0) == 2534.0 + 60.0 * 200
+    assert bench.step_bytes("plain", 200, 0, diffuse_depth=2) == 2534.0 - 800.0 + 60.0 * 200  # two sweeps per pass
     assert bench.STAGE_BYTES["pcg_matvec"] + bench.STAGE_BYTES["pcg_update"] == 60.0
     assert 40.0 < bench.MEASURED_TRAFFIC_PER_CELL["pcg_matvec"] < 41.0
     # the scope table's model of the same step: 2558 B of stages + 52 B per matrix-free iteration

@@ -24,16 +24,22 @@ writes, equal substep counts, PCG iteration counts within one. The ground stage 
 Boundary masks: the Neigh records of computeNeighbourGPU (Game/kernelSky.cu:1284-1316) against
 the classes the library's kernels derive from the heightfield (skt_read_neighbours), bit for bit,
 on flat ground and on a heightfield with interior hills and ground at the domain edges.
+
+Step time: the reference's kernels as its updateGPU drives them (the harness synchronises the
+context after launches as the reference does) against this library, each step one launch of its
+captured graph, on the same grids from the same initial state: the reference GPU baseline.
 """
 import copy
 import json
 import os
+import time
 
 import numpy as np
 import pytest
 
 import oracle
 from helpers import GROUND, SKY, make_env, oracle_cfg, push_oracle_to_env, rel_l2, rel_max, small_case
+from skewtcloudsim_gb300 import SolverConfig
 
 pytestmark = pytest.mark.gpu
 
@@ -61,7 +67,7 @@ GRIDS = _grids() or [pytest.param(None, marks=pytest.mark.skip("no reference cub
 
 
 def _record(name, data):
-    """Writes the per-step distances to $SKT_REPORT_DIR/refparity_<grid>.json when that folder is set."""
+    """Writes a report (per-step distances, step times) to $SKT_REPORT_DIR/refparity_<name>.json when that folder is set."""
     d = os.environ.get("SKT_REPORT_DIR", "")
     if d and os.path.isdir(d):
         with open(os.path.join(d, f"refparity_{name}.json"), "w") as f:
@@ -236,3 +242,37 @@ def test_boundary_masks_bit_exact(gpu_lib, grid, terrain):
     assert diff.size == 0, (diff[:10], want[diff[:3]], got[diff[:3]])
     if terrain:
         assert (want[:, :, 1] == 1).sum() > 0  # the masks do see ground neighbours
+
+
+@pytest.mark.parametrize("grid", GRIDS)
+def test_step_time_against_reference_kernels(gpu_lib, grid):
+    """Wall time per step (device synchronised) over ten steps: the reference's kernels through the
+    harness, the per-call upload and readback taken out as (T(10 steps) - T(1 step)) / 9, against
+    the library in graph mode. Both start from the same initial state; the PCG iteration counts
+    are recorded beside the times (the reference's state turns unsound on grids wider than 16, and
+    its PCG then runs to the cap). Written to $SKT_REPORT_DIR/refparity_time_<grid>.json when set."""
+    X, Y, Z = grid
+    init, dt, speed = small_case((X, Z, Y))
+    n = 10
+    ref = oracle.OracleState(init, np.float32)
+    refh.run_reference(ref, dt, speed, 1)  # module load and first allocations
+    t0 = time.perf_counter()
+    refh.run_reference(ref, dt, speed, 1)
+    t1 = time.perf_counter()
+    rn = refh.run_reference(ref, dt, speed, n)
+    t2 = time.perf_counter()
+    ref_ms = ((t2 - t1) - (t1 - t0)) / (n - 1) * 1e3
+    env = make_env(init, SolverConfig(use_graph=1))
+    env.update_gpu(dt, speed)  # capture
+    env.sync()
+    t3 = time.perf_counter()
+    env.update_gpu(dt, speed, nsteps=n)
+    env.sync()
+    ours_ms = (time.perf_counter() - t3) / n * 1e3
+    st = env.stats()
+    env.close()
+    _record(f"time_{X}x{Y}x{Z}", {"grid_ref_layout": [X, Y, Z], "steps": n, "reference_ms_per_step": ref_ms,
+                                  "library_ms_per_step": ours_ms, "speedup": ref_ms / ours_ms,
+                                  "reference_pcg_iters": rn["pcg_iters"], "library_pcg_iters_last_step": st["pcg_iters"],
+                                  "library_kernel_launches": st["kernel_launches"]})
+    assert ours_ms < ref_ms, (ours_ms, ref_ms)
