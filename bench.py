@@ -293,7 +293,7 @@ def mode_config(args, mode):
     return SolverConfig(semantics=1, precision=1, mg_half=args.mg_half, pcg_fused=args.pcg_fused, use_graph=g)
 
 
-def survey_step_bytes(mode, pcg_iters, outer):
+def scope_step_bytes(mode, pcg_iters, outer):
     """The scope table's algorithmic model of a cell-step: 2558 B of stages plus 52 B per Jacobi-PCG
     iteration (matrix-free: the operator's coefficients formed from the density, 4 B, instead of
     four stored coefficient arrays, 16 B) plus 40 B per refinement step. The library streams the
@@ -506,7 +506,7 @@ def main():
                   "model": (f"the library's own bytes: {stage_bytes(depth):.0f} B of stages (diffusion at {depth} sweep(s) per "
                             "pass) + 60 B per plain PCG iteration (stored coefficients)")}
     if head["mode"] != "mixed":
-        sb = survey_step_bytes(head["mode"], head["pcg_iters"], head["outer"])
+        sb = scope_step_bytes(head["mode"], head["pcg_iters"], head["outer"])
         step_model["scope_model"] = {
             "bytes_per_cell_step": sb, "frac": round(sb * head["value"] / 1e9 / peak, 4),
             "model": "2558 B of stages + 52 B per matrix-free Jacobi-PCG iteration; the library streams four stored "
@@ -590,7 +590,7 @@ def main():
             "step_roofline": {"bytes_per_cell_step": step_bytes("plain", t["pcg_iters"], 0, t["tuning"].get("diffuse_depth", 1)),
                               "frac": round(step_bytes("plain", t["pcg_iters"], 0, t["tuning"].get("diffuse_depth", 1)) * t["value"]
                                             / 1e9 / peak, 4),
-                              "scope_model_frac": round(survey_step_bytes("plain", t["pcg_iters"], 0) * t["value"] / 1e9 / peak, 4)},
+                              "scope_model_frac": round(scope_step_bytes("plain", t["pcg_iters"], 0) * t["value"] / 1e9 / peak, 4)},
             "profile_ms": {k: round(v["ms"], 3) for k, v in t["prof"].items()}}
     if "mixed" in res and head["mode"] != "mixed":
         m = res["mixed"]

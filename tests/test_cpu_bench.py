@@ -30,4 +30,4 @@ def test_step_byte_model():
     assert bench.STAGE_BYTES["pcg_matvec"] + bench.STAGE_BYTES["pcg_update"] == 60.0
     assert 40.0 < bench.MEASURED_TRAFFIC_PER_CELL["pcg_matvec"] < 41.0
     # the scope table's model of the same step: 2558 B of stages + 52 B per matrix-free iteration
-    assert bench.survey_step_bytes("plain", 200, 0) == 2558.0 + 52.0 * 200
+    assert bench.scope_step_bytes("plain", 200, 0) == 2558.0 + 52.0 * 200
