@@ -360,6 +360,19 @@ def run_mode(args, mode, init, dt, speed, cells, world, local, pg, torch):
             "pcg_max_iter": cfg.pcg_max_iter}
 
 
+def ensemble_tuning(args, envs):
+    """Launch shapes of the members: --tuning's values for all, else the defaults at the members' SM
+    shares. (Measured on the 48 members: 100.3 ms per ensemble step with the defaults, 101.6 ms with
+    each size's autotuned shapes, which the tuner measures on a member running alone, 103.5 and
+    105.5 ms with two-sweep diffusion of 14 and 6 rows.) The shapes never change a member's bits."""
+    if args.tuning:
+        kv = {k: int(v) for k, v in (item.split("=") for item in args.tuning.split(","))}
+        for e in envs:
+            e.set_tuning(**kv)
+        return dict(kv, source="--tuning")
+    return {"source": "defaults at the ensemble SM shares"}
+
+
 def run_ensemble(args, rank, world, local, pg, torch):
     """The batched ensemble (``--workload ensemble-48``): 48 members of uneven sizes drawn from
     {64x64x32, 96x96x64, 128x128x64, 192x192x96}, each with its own seeded sounding and bubble, all
@@ -379,6 +392,7 @@ def run_ensemble(args, rank, world, local, pg, torch):
     cells = sum(m[0].n for m in members)
     from skewtcloudsim_gb300 import Ensemble
     ens = Ensemble(envs) if args.ensemble_runner == "graph" else None
+    tuning = ensemble_tuning(args, envs)
 
     def advance(k):
         if ens is not None:
@@ -428,7 +442,7 @@ def run_ensemble(args, rank, world, local, pg, torch):
                        "concurrency": ("one CUDA graph launch per ensemble step, every member's whole step an independent "
                                        "branch (loops as device-side conditional nodes)" if ens is not None
                                        else "one host thread per member, one stream per member"),
-                       "host_thread_runner_ms_per_step": other,
+                       "host_thread_runner_ms_per_step": other, "tuning": tuning,
                        "sequential_ms_per_step": seq * 1e3, "parallelism": "single" if world == 1 else f"replicas{world}"},
             "gpu_launches": launches, "clocks": clk.summary()}), flush=True)
     return 0
