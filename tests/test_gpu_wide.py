@@ -202,3 +202,25 @@ def test_c2_one_step(gpu_lib):
     assert abs(gd["pcg_iters"] - od["pcg_iters"]) <= 1, (gd, od)
     bad = {k: v for k, v in res.items() if v[0] > STEP_TOL}
     assert not bad, bad
+
+
+def test_c3_one_step_benchmarked_configuration(gpu_lib):
+    """One whole step of the precision-512x512x256 workload at its full size (67.1M cells), in the
+    configuration the benchmark runs (the step as one graph launch, two-sweep diffusion passes of
+    14-row tiles with 4 blocks per SM, the tuned PPM run lengths) against the oracle on the host
+    cores (about a minute on 16 cores): relative L2 <= 1e-5 on every field, equal substep counts,
+    PCG iteration counts within one."""
+    from skewtcloudsim_gb300 import SolverConfig
+    init, dt, speed = small_case((512, 512, 256), name=WORKLOAD)
+    env = make_env(init, SolverConfig(use_graph=1))
+    env.set_tuning(diffuse_depth=2, diffuse_rows=14, diffuse2_bps=4, ppm_x_bps=8, ppm_y_bps=32, ppm_z_bps=8)
+    env.update_gpu(dt, speed)
+    gd = env.stats()
+    st = oracle.OracleState(init, np.float32)
+    od = st.step(oracle_cfg(), dt, speed)
+    res = compare(env, st)
+    env.close()
+    assert gd["nsub"] == od["nsub"], (gd, od)
+    assert abs(gd["pcg_iters"] - od["pcg_iters"]) <= 1, (gd, od)
+    bad = {k: v for k, v in res.items() if v[0] > STEP_TOL}
+    assert not bad, bad
