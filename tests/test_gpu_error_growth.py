@@ -1,7 +1,8 @@
 """Error growth of the GPU step against the FP64 oracle of the same method, free running.
 
 Both runs start from the same state and are never re-synchronised. After N steps (50 by default,
-SKT_ERR_STEPS overrides; run with -s to print the per-field table) every sky field's relative L2
+SKT_ERR_STEPS overrides; the grid is 32x32x32, SKT_ERR_SHAPE=x,y,z (z vertical) overrides; run with
+-s to print the per-field table) every sky field's relative L2
 distance from the FP64 oracle is compared with that of the FP32 oracle (the same method in FP32):
 FP32 storage of the fields alone makes the two FP64 and FP32 trajectories drift apart (theta by
 ~1.4e-6 per step: the diffusion increments k*dtheta ~ 1e-7 K are below one ulp of theta ~ 300 K),
@@ -25,7 +26,7 @@ from skewtcloudsim_gb300 import SolverConfig
 
 pytestmark = pytest.mark.gpu
 
-SHAPE = (32, 32, 32)
+SHAPE = tuple(int(v) for v in os.environ.get("SKT_ERR_SHAPE", "32,32,32").split(","))
 STEPS = int(os.environ.get("SKT_ERR_STEPS", "50"))
 REPORT = sorted({1, 10, STEPS // 2, STEPS} - {0})
 

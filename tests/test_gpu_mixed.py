@@ -3,7 +3,8 @@ refinement) against the FP64 oracle of the same (textbook) method solved to a ti
 
 The FP64 oracle runs the projection with Jacobi-PCG in double precision until the max residual
 is below 1e-13; the GPU solves the same symmetric system to a relative FP64 residual of 1e-8.
-Tolerances: relative L2 <= 1e-6 on u, v, w, p, rho after one projection; <= 1e-5 on every field
+Tolerances: relative L2 <= 1e-6 on u, v, w, p, rho after one projection (v: or 1.5x the FP32
+oracle's own distance on the same projection, whichever is larger); <= 1e-5 on every field
 after each of three whole steps started from identical inputs, except the vertical wind v: its
 FP32 rounding alone (buoyancy differences of ~300 K virtual temperatures, and v is an order of
 magnitude smaller than u and w) gives ~1.4e-5, which the FP32 oracle shows too, so v must stay
@@ -57,6 +58,8 @@ def _developed(shape):
 
 def _check_projection(init, dt, speed, st32, cfg, max_inner=None):
     ref = _to64(st32, init)
+    f32 = _to32(ref, init)  # the same projection by the FP32 oracle: v's own FP32 floor
+    f32.stage(oracle.Config(semantics=1, pcg_tol=1e-9, pcg_max_iter=5000), 3, 0, dt * speed)
     env = make_env(init, cfg)
     push_oracle_to_env(st32, env)
     g = env.run_stage(3, 0, dt * speed)
@@ -70,7 +73,8 @@ def _check_projection(init, dt, speed, st32, cfg, max_inner=None):
     m = ref.sky_mask()
     for k in ("u", "v", "w", "p", "rho"):
         e = rel_l2(env.read(k), ref.a[k], m)
-        assert e <= 1e-6, (k, e, g, st)
+        limit = 1e-6 if k != "v" else max(1e-6, 1.5 * rel_l2(f32.a[k], ref.a[k], m))
+        assert e <= limit, (k, e, limit, g, st)
     env.close()
 
 
@@ -89,6 +93,16 @@ def test_mixed_projection_hierarchies(gpu_lib, shape, max_inner):
     itself and the unfused residual kernel sets the inner tolerance from its max |r|."""
     init, dt, speed, st32 = _developed(shape)
     _check_projection(init, dt, speed, st32, SolverConfig(precision=1, refine_tol=1e-8), max_inner)
+
+
+def test_mixed_projection_c2_matches_fp64(gpu_lib):
+    """The plain-256x256x128 workload at its full size (8.4M cells: a vector finest level and
+    vector coarse levels of 128x64x128 .. 16x8x16), after one oracle step: the projection against
+    the FP64 oracle solved to 1e-13 (about half a minute on 16 cores)."""
+    init, dt, speed = small_case((256, 256, 128), name="plain-256x256x128")
+    st = oracle.OracleState(init, np.float32)
+    st.step(oracle.Config(semantics=1), dt, speed)
+    _check_projection(init, dt, speed, st, SolverConfig(precision=1, refine_tol=1e-8), 60)
 
 
 def test_mixed_steps_match_fp64(gpu_lib):
