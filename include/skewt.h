@@ -133,7 +133,15 @@ skt_status skt_init(skt_env* env, const float* theta, const float* vel_aos3, con
  * Game/environment.cu:553, is explicit here: skt_read_field). */
 skt_status skt_step(skt_env* env, float dt, float speed, int nsteps);
 
-/* Waits for the environment's stream. */
+/* skt_step without waiting (graph mode, cfg.use_graph = 1): queues nsteps launches of the captured
+ * step on the environment's stream and returns; the host may work meanwhile, and further calls
+ * queue more steps. skt_sync waits for them and returns what skt_step would have returned for all
+ * of them (SKT_NOT_CONVERGED, SKT_NAN_DETECTED, ...); skt_stats describes them after skt_sync.
+ * Field reads, writes and edits queue behind the steps on the same stream. Without graph mode the
+ * steps read their loop counts on the host, and the call runs them as skt_step does. */
+skt_status skt_step_async(skt_env* env, float dt, float speed, int nsteps);
+
+/* Waits for the environment's stream; after skt_step_async, the status of the queued steps. */
 skt_status skt_sync(skt_env* env);
 
 /* Ensemble stepping: advances n independent environments (members of any grid sizes, each with

@@ -48,6 +48,7 @@ SIGNATURES = {
                                 c_float_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32, ctypes.c_uint32]),
     "skt_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_int]),
     "skt_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "skt_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_int]),
     "skt_step_ensemble": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, c_float_p, ctypes.c_float, c_float_p,
                                          ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "skt_read_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_float_p, ctypes.c_size_t]),

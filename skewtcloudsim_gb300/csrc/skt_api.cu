@@ -331,26 +331,50 @@ skt_status graph_status(Env& e) {
 }
 
 // nsteps launches of the captured step; the host reads the solver scalars once at the end
-skt_status step_graph(Env& e, float dt, float speed, int nsteps) {
-    if (!e.graph_exec || !same_key(e.gkey, graph_key(e, dt, speed))) {
-        const skt_status st = capture_step(e, dt, speed);
-        if (st != SKT_OK) return st;
-    }
-    if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
-    cudaEventRecord(e.ev0, e.stream);
-    for (int i = 0; i < nsteps; ++i) {
-        const skt_status ps = prepare_launch(e, e.graph_exec, e.book, e.stream);
-        if (ps != SKT_OK) return ps;
-        if (cudaGraphLaunch(e.graph_exec, e.stream) != cudaSuccess) return cuda_check(e, "graph launch");
-        advance_clock(e, dt, speed);
-    }
+// Waits for the graph steps queued by skt_step_async and accounts for them (solver scalars, stats,
+// kernel count, device time since the first of them); the status they left on the device.
+skt_status collect_async(Env& e) {
+    if (e.async_steps == 0) return SKT_OK;
+    const int n = e.async_steps;
+    e.async_steps = 0;
     cudaEventRecord(e.ev1, e.stream);
     cudaEventSynchronize(e.ev1);
     cudaEventElapsedTime(&e.last_gpu_ms, e.ev0, e.ev1);
     const skt_status st = cuda_check(e, "graph step");
     if (st != SKT_OK) return st;
-    finish_graph_steps(e, e.book, nsteps);
+    finish_graph_steps(e, e.book, n);
+    return graph_status(e);
+}
+
+// Queues nsteps launches of the captured step (capturing it first when dt, speed, the terrain's
+// flatness, the diagnostics or the tuning changed); the steps are collected by collect_async.
+skt_status launch_graph_steps(Env& e, float dt, float speed, int nsteps) {
+    if (!e.graph_exec || !same_key(e.gkey, graph_key(e, dt, speed))) {
+        // a new capture replaces the graph and its bookkeeping: collect what the old one queued
+        if (e.async_steps > 0) {
+            const skt_status pst = collect_async(e);
+            if (pst != SKT_OK && pst != SKT_NOT_CONVERGED) return pst;
+        }
+        const skt_status st = capture_step(e, dt, speed);
+        if (st != SKT_OK) return st;
+    }
+    if (!e.ev0) { cudaEventCreate(&e.ev0); cudaEventCreate(&e.ev1); }
+    if (e.async_steps == 0) cudaEventRecord(e.ev0, e.stream);
+    for (int i = 0; i < nsteps; ++i) {
+        const skt_status ps = prepare_launch(e, e.graph_exec, e.book, e.stream);
+        if (ps != SKT_OK) return ps;
+        if (cudaGraphLaunch(e.graph_exec, e.stream) != cudaSuccess) return cuda_check(e, "graph launch");
+        advance_clock(e, dt, speed);
+        ++e.async_steps;
+    }
     return SKT_OK;
+}
+
+skt_status step_graph(Env& e, float dt, float speed, int nsteps) {
+    const skt_status st = launch_graph_steps(e, dt, speed, nsteps);
+    if (st != SKT_OK) return st;
+    const skt_status cs = collect_async(e);
+    return cs == SKT_NOT_CONVERGED ? SKT_OK : cs;  // skt_step turns the solver state into its status
 }
 
 }  // namespace
@@ -687,6 +711,11 @@ skt_status skt_step(skt_env* env, float dt, float speed, int nsteps) {
     Env& e = env->e;
     if (!e.initialized) return fail(&e, SKT_NOT_INITIALIZED, "skt_init has not run");
     if (!(dt > 0.0f) || !(speed > 0.0f) || nsteps < 0) return fail(&e, SKT_INVALID_ARG, "dt and speed must be > 0, nsteps >= 0");
+    if (e.async_steps > 0 && !(e.cfg.use_graph && !e.prof && nsteps > 0)) {
+        // stream-ordered steps after graph steps queued by skt_step_async: collect those first
+        const skt_status ps = collect_async(e);
+        if (ps != SKT_OK && ps != SKT_NOT_CONVERGED) return ps;
+    }
     if (e.cfg.use_graph && !e.prof && nsteps > 0) {
         // graph mode: the status is read once after the nsteps launches
         const skt_status gs = step_graph(e, dt, speed, nsteps);
@@ -934,8 +963,19 @@ skt_status skt_step_ensemble(skt_env* const* envs, int n, const float* dt, float
 
 skt_status skt_sync(skt_env* env) {
     if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    if (env->e.async_steps > 0) return collect_async(env->e);
     cudaStreamSynchronize(env->e.stream);
     return cuda_check(env->e, "sync");
+}
+
+skt_status skt_step_async(skt_env* env, float dt, float speed, int nsteps) {
+    if (!env) return fail(nullptr, SKT_INVALID_ARG, "null env");
+    Env& e = env->e;
+    if (!e.initialized) return fail(&e, SKT_NOT_INITIALIZED, "skt_init has not run");
+    if (!(dt > 0.0f) || !(speed > 0.0f) || nsteps < 0) return fail(&e, SKT_INVALID_ARG, "dt and speed must be > 0, nsteps >= 0");
+    if (!e.cfg.use_graph || e.prof) return skt_step(env, dt, speed, nsteps);  // stream-ordered steps read their loop counts on the host
+    if (nsteps == 0) return SKT_OK;
+    return launch_graph_steps(e, dt, speed, nsteps);
 }
 
 skt_status skt_read_field(skt_env* env, int param, int dir, float* dst, size_t n) {

@@ -248,6 +248,7 @@ struct Env {
     // launch accounting and optional per-stage event timing
     long long launches = 0;
     float last_gpu_ms = 0.0f;
+    int async_steps = 0;  // graph steps queued by skt_step_async and not yet collected by skt_sync
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool prof = false;
     struct ProfRec { const char* name; cudaEvent_t a, b; int nk; };

@@ -190,8 +190,13 @@ class Environment:
         """environmentGPU::updateGPU (Game/environment.cu:391-555); NOT_CONVERGED is returned, not raised."""
         return self._check(self._L.skt_step(self._h, dt, speed, nsteps), allow=(Status.NOT_CONVERGED,))
 
-    def sync(self):
-        self._check(self._L.skt_sync(self._h))
+    def update_gpu_async(self, dt: float, speed: float = 1.0, nsteps: int = 1) -> Status:
+        """skt_step_async: queues the steps (graph mode) and returns; sync() collects them."""
+        return self._check(self._L.skt_step_async(self._h, dt, speed, nsteps), allow=(Status.NOT_CONVERGED,))
+
+    def sync(self) -> Status:
+        """skt_sync: waits; after update_gpu_async, the queued steps' status (NOT_CONVERGED is returned, not raised)."""
+        return self._check(self._L.skt_sync(self._h), allow=(Status.NOT_CONVERGED,))
 
     def get_param_array(self, parameter: int, direction: int = Direction.RIGHT) -> int:
         """environmentGPU::getParamArray: device address of the field (int)."""

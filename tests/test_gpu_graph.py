@@ -86,3 +86,30 @@ def test_graph_reports_nan(gpu_lib):
         env.update_gpu(dt, speed)
     assert ei.value.status == Status.NAN_DETECTED
     env.close()
+
+
+def test_async_steps_equal_synchronous_steps(gpu_lib):
+    """skt_step_async queues graph steps without waiting and skt_sync collects them: three queued
+    single steps give the fields, counts, clock and status of one three-step skt_step; a new dt
+    between queued calls captures again after collecting what the old graph queued; a synchronous
+    step after queued ones collects them first; a NaN met by a queued step is reported by skt_sync."""
+    init, dt, speed, a, c = _pair((32, 32, 32), dict(semantics=0))
+    ra = a.update_gpu(dt, speed, nsteps=3)
+    for _ in range(3):
+        assert c.update_gpu_async(dt, speed) == Status.OK
+    assert c.sync() == ra
+    _same(a, c, "three queued steps")
+    a.update_gpu(2 * dt, speed)
+    a.update_gpu(dt, speed)
+    c.update_gpu_async(dt * 2, speed)  # a new dt: a new capture
+    c.update_gpu(dt, speed)            # synchronous, after a queued step of another dt
+    _same(a, c, "new dt, then a synchronous step")
+    u = c.read("u")
+    u[16 + 10 * 32 + 16 * 32 * 32] = np.nan
+    c.write("u", u)
+    assert c.update_gpu_async(dt, speed) == Status.OK  # queued: nothing is known yet
+    with pytest.raises(SktError) as ei:
+        c.sync()
+    assert ei.value.status == Status.NAN_DETECTED
+    a.close()
+    c.close()
