@@ -55,6 +55,16 @@ public:
         return true;
     }
 
+    // updateGPU without waiting (graph mode): the steps are queued; sync() collects them and
+    // returns false when a pressure solve among them hit its iteration cap.
+    void updateGPUAsync(float dt, float speed, int nsteps = 1) { check(skt_step_async(env_, dt, speed, nsteps)); }
+    bool sync() {
+        const skt_status s = skt_sync(env_);
+        if (s == SKT_NOT_CONVERGED) return false;
+        check(s);
+        return true;
+    }
+
     // environmentGPU::getParamArray
     float* getParamArray(skt_param type, skt_direction windDir = SKT_RIGHT) {
         float* p = nullptr;
