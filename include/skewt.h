@@ -183,9 +183,11 @@ skt_status skt_read_field(skt_env* env, int param, int dir, float* host_dst, siz
  * work queued so far are snapshot on the device, then copied to host_dsts[i] on a second stream,
  * so that the next steps can run while the copies proceed; the call returns at once. A new
  * snapshot first waits for the previous one's copies. The host buffers (n floats each, n =
- * nx*ny*nz) must stay valid until skt_read_wait. Pinned buffers (cudaHostAlloc /
- * cudaHostRegister) are written by a small kernel through their mapped addresses, alongside the
- * next steps' kernels; pageable buffers are copied by the copy engine.
+ * nx*ny*nz) must stay valid until skt_read_wait. In graph mode (cfg.use_graph = 1) every buffer is
+ * copied by the copy engine, beside the next steps; with stream-ordered steps, whose small scalar
+ * reads would queue behind those copies, pinned buffers (cudaHostAlloc / cudaHostRegister) are
+ * written by a small kernel through their mapped addresses instead, alongside the next steps'
+ * kernels, and pageable ones by the copy engine.
  * The snapshot memory (nfields fields) is allocated by the first call that needs it. */
 skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, const int* dirs, float* const* host_dsts,
                                  size_t n);

@@ -1038,13 +1038,18 @@ skt_status skt_read_fields_async(skt_env* env, int nfields, const int* params, c
     }
     cudaEventRecord(e.ev_snap, e.stream);
     cudaStreamWaitEvent(e.copy_stream, e.ev_snap, 0);
-    // pinned destinations are written by a narrow kernel through their mapped addresses (it takes a
-    // few SMs beside the next step's kernels); pageable ones by the copy engine
+    // Stream-ordered steps read small scalars back through the copy engine and would queue behind
+    // bulk copies there: for them, pinned destinations are written by a narrow kernel through
+    // their mapped addresses (it takes a few SMs beside the next step's kernels). Graph steps read
+    // nothing back until the call ends, so the copy engine takes every field and leaves the SMs to
+    // the step (measured at 512x512x256: a step beside the readback 163.7 ms with the copy engine,
+    // 166.5 ms with the writer kernel, 162.7 ms alone). Pageable destinations: the copy engine.
+    const bool writer_kernel = !e.cfg.use_graph || e.prof;
     for (int i = 0; i < nfields; ++i) {
         const float* s = e.snap + size_t(i) * n;
         cudaPointerAttributes at{};
-        const bool known = cudaPointerGetAttributes(&at, dst[i]) == cudaSuccess;
-        if (!known) cudaGetLastError();  // an unregistered host pointer: clear only the query's own error
+        const bool known = writer_kernel && cudaPointerGetAttributes(&at, dst[i]) == cudaSuccess;
+        if (writer_kernel && !known) cudaGetLastError();  // an unregistered host pointer: clear only the query's own error
         const bool mapped = known && at.type == cudaMemoryTypeHost && at.devicePointer &&
                             (reinterpret_cast<uintptr_t>(at.devicePointer) % 16) == 0 && n % 4 == 0;
         if (mapped) {
