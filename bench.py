@@ -565,8 +565,9 @@ def main():
                "d2h_bytes_per_step": int(d2h), "steps": K,
                "note": "init from pinned host arrays once, then after each step the readback of the 11 "
                        "prognostic fields into pinned host arrays (the reference's per-step GPUSetEnv), "
-                       "snapshot on the device and written into the pinned arrays by a kernel on a second "
-                       "stream during the next step; host wall clock from the start of the upload up to the "
+                       "snapshot on the device and copied into the pinned arrays on a second stream during the "
+                       "next step (the copy engine in graph mode, a writer kernel otherwise); host wall clock "
+                       "from the start of the upload up to the "
                        "last step's copies; the environment's graph was captured by one untimed step before"}
         env2.close()
 
