@@ -553,16 +553,23 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         upload()
+        t_up = time.perf_counter()
         host_outs = {k: outs[k][0] for k in names}
+        step_ms = []
         for _ in range(K):
+            ts = time.perf_counter()
             env2.update_gpu(dt, speed)
             env2.read_async(host_outs)  # this step's fields copy out while the next step runs
+            step_ms.append(round((time.perf_counter() - ts) * 1e3, 1))
+        tw = time.perf_counter()
         env2.read_wait()
         el = time.perf_counter() - t0
         h2d = sum(a[0].nbytes for a in host_in.values()) + init.ground_height.nbytes
         d2h = len(names) * cells * 4
         e2e = {"value": cells * K / el, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d / K),
                "d2h_bytes_per_step": int(d2h), "steps": K,
+               "phases_ms": {"upload": round((t_up - t0) * 1e3, 1), "steps": step_ms,
+                             "last_readback": round((time.perf_counter() - tw) * 1e3, 1)},
                "note": "init from pinned host arrays once, then after each step the readback of the 11 "
                        "prognostic fields into pinned host arrays (the reference's per-step GPUSetEnv), "
                        "snapshot on the device and copied into the pinned arrays on a second stream during the "
