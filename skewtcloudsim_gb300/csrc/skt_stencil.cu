@@ -491,7 +491,6 @@ __global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
         }
     };
     auto nxt = [](int s) { return s + 1 == P4SLOTS ? 0 : s + 1; };
-    // first sweep of plane p for a row warp: ib, ic the input planes p-1, p; s0, s1 the slots of p, p+1
     // x neighbours of a lane's four cells c from the shared row (at the warp's ends the edge warp's
     // cells), at the grid's ends the ghost. (Warp shuffles for the inner lanes measured slower: the
     // end lanes' loads become divergent branches.)
@@ -499,7 +498,9 @@ __global__ void __launch_bounds__(32 * (R + 3), p4_min_blocks<R>())
         l = lfix ? side_val(sides, c.x, dy) : row[-1];
         r = rfix ? side_val(sides, c.w, dy) : row[4];
     };
-    // dg: the value below row 1 (theta's ground face of the plane, else the ground ghost)
+    // first sweep of plane p for a row warp: ib, ic the input planes p-1, p; s0, s1 the slots of p,
+    // p+1; f gets the input plane p+1; dg: the value below row 1 (theta's ground face of the plane,
+    // else the ground ghost)
     auto sweep1 = [&](bool gen, int p, const float4& ib, const float4& ic, int s0, int s1, float4& f, const float4& dg) {
         const float* row = ring + s0 * SLOTF + own;
         f = ld4s(ring + s1 * SLOTF + own);
