@@ -37,11 +37,11 @@ long long dir_read(void* ctx, const char* name, char* buf, size_t cap) {
 }
 
 struct Args {
-    std::string knmi, dwd, dir, raw;
+    std::string knmi, dwd, dir, raw, tune;
     int nx = 64, ny = 32, nz = 64;
     float voxel = 100.0f, dt = 0.5f, speed = 1.0f;
     int steps = 10;
-    bool mixed = false, textbook = false, noise = true, parse_only = false;
+    bool mixed = false, textbook = false, noise = true, parse_only = false, graph = false;
     unsigned seed = 100;
 };
 
@@ -50,7 +50,7 @@ struct Args {
                  "skt_run: %s\n"
                  "usage: skt_run --knmi DIR | --dwd ARCHIVE_NAME --dir DIR [--grid NX,NY,NZ] [--voxel M] [--steps N]\n"
                  "               [--dt S] [--speed F] [--mixed] [--textbook] [--no-noise] [--seed K] [--raw OUTDIR]\n"
-                 "               [--parse-only]\n",
+                 "               [--graph] [--tune CACHE_FILE] [--parse-only]\n",
                  msg);
     std::exit(2);
 }
@@ -78,6 +78,8 @@ Args parse(int argc, char** argv) {
         else if (k == "--textbook") a.textbook = true;
         else if (k == "--no-noise") a.noise = false;
         else if (k == "--parse-only") a.parse_only = true;
+        else if (k == "--graph") a.graph = true;  // each step one launch of the captured CUDA graph
+        else if (k == "--tune") a.tune = val();   // the autotuner's launch shapes, cached in this file
         else usage(("unknown option " + k).c_str());
     }
     if (a.knmi.empty() == (a.dwd.empty())) usage("give exactly one of --knmi and --dwd");
@@ -117,10 +119,18 @@ int main(int argc, char** argv) {
         skt_default_config(&cfg);
         cfg.precision = a.mixed ? SKT_PCG_MIXED : SKT_PCG_PLAIN;
         cfg.semantics = a.textbook ? SKT_SEM_TEXTBOOK : SKT_SEM_REFERENCE;
+        cfg.use_graph = a.graph ? 1 : 0;
         skewt::EnvironmentGPU env(a.nx, a.ny, a.nz, a.voxel, &cfg);
         table.initEnvironment(env, a.noise, a.seed);
         std::printf("{\"sounding_rows\": %zu, \"grid\": [%d, %d, %d], \"voxel\": %g, \"precision\": \"%s\", \"semantics\": \"%s\"}\n",
                     table.data().n, a.nx, a.ny, a.nz, a.voxel, a.mixed ? "mixed" : "plain", a.textbook ? "textbook" : "reference");
+        if (!a.tune.empty()) {
+            skt_tuning t{};
+            const skt_status ts = skt_autotune(env.handle(), a.tune.c_str(), 0, &t);
+            if (ts != SKT_OK) throw skewt::Error(ts, skt_last_error(env.handle()));
+            std::printf("{\"tuning\": {\"diffuse_depth\": %d, \"diffuse_rows\": %d, \"from_cache\": %s}}\n", t.diffuse_depth,
+                        t.diffuse_rows, t.from_cache ? "true" : "false");
+        }
         const double cells = double(a.nx) * a.ny * a.nz;
         double gpu_ms = 0.0;
         const auto t0 = std::chrono::steady_clock::now();

@@ -1,6 +1,7 @@
 """The skt_run driver (host C++ over the C ABI) steps the same atmosphere as the Python path: the
 same KNMI sounding, grid and solver settings give the same 11 prognostic fields, bit for bit,
-after a few steps, in both projection modes."""
+after a few steps, in both projection modes; and the driver's fast path (each step one graph
+launch, the autotuner's launch shapes) gives the same bits as the Python path's default one."""
 import json
 import subprocess
 import zipfile
@@ -15,8 +16,8 @@ pytestmark = pytest.mark.gpu
 NAMES = ("th", "qv", "qw", "qc", "qr", "qs", "qi", "u", "v", "w", "p")
 
 
-@pytest.mark.parametrize("mixed", [False, True])
-def test_driver_matches_python_path(gpu_lib, tmp_path, mixed):
+@pytest.mark.parametrize("mixed,fast", [(False, False), (True, False), (False, True)], ids=["plain", "mixed", "graph-tuned"])
+def test_driver_matches_python_path(gpu_lib, tmp_path, mixed, fast):
     from skewtcloudsim_gb300 import Environment, SolverConfig, build, radiosonde
     driver = build.build_driver()
     path = sf.write_knmi(str(tmp_path), "fine", 3)
@@ -27,10 +28,13 @@ def test_driver_matches_python_path(gpu_lib, tmp_path, mixed):
     out.mkdir()
     nx, ny, nz, steps = 32, 24, 32, 3
     args = [driver, "--knmi", str(members), "--grid", f"{nx},{ny},{nz}", "--steps", str(steps), "--dt", "0.5",
-            "--raw", str(out)] + (["--mixed"] if mixed else [])
+            "--raw", str(out)] + (["--mixed"] if mixed else []) + (["--graph", "--tune", str(tmp_path / "tune.json")] if fast else [])
     r = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     lines = [json.loads(s) for s in r.stdout.strip().splitlines()]
+    if fast:
+        assert "tuning" in lines[1] and not lines[1]["tuning"]["from_cache"]
+        lines = lines[:1] + lines[2:]
     assert lines[0]["grid"] == [nx, ny, nz] and len(lines) == steps + 2
     assert all(l["pcg_iters"] > 0 for l in lines[1:-1]) and lines[-1]["cell_steps_per_s"] > 0
 
